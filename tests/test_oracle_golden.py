@@ -1,0 +1,108 @@
+"""The FP64 CPU oracle against the reference's own golden vectors.
+
+Fixtures (tests/golden/, extracted from the reference by make_golden.py):
+  * Si.soap.cur_points.json  -- 100 SOAP vectors, reference tolerance 1e-8
+    (tests/test_gapfit.py:58, config :93-95)
+  * test_descriptor.py       -- C2H SOAP gradient values and index table, tol 1e-7
+    (tests/test_descriptor.py:68-190, :211-226)
+  * test_gappot.py           -- distance_2b GAP energy (1e-5) and forces (1e-6)
+  * test_potential_cell.py   -- H2 in cells 2.5..4.5 A, cutoff 4 > cell, tol 1e-6
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from quip_gb300.atoms import read_xyz
+
+SI_SOAP = ("soap atom_sigma=0.5 central_weight=1.0 cutoff=4.0 cutoff_transition_width=1.0 "
+           "l_max=8 n_max=8 n_species=1 species_Z={14} Z=14")
+
+
+def test_si_soap_cur_points(golden):
+    frames = read_xyz(os.path.join(golden, "Si.np1.xyz"))
+    ref = np.load(os.path.join(golden, "si_soap_cur_points.npz"))
+    X, idx = ref["sparsex"], ref["index"]
+    assert X.shape == (100, 325)
+    # global 1-based atom index -> (frame, atom)
+    where = [(f, k) for f, fr in enumerate(frames) for k in range(len(fr))]
+    assert len(where) == 439
+    per_frame = {}
+    for t, gi in enumerate(idx):
+        f, k = where[gi - 1]
+        per_frame.setdefault(f, []).append((t, k))
+    worst = 0.0
+    for f, items in per_frame.items():
+        fr = frames[f]
+        q = oracle.soap(SI_SOAP, fr.positions, fr.numbers, fr.lattice, fr.pbc)
+        for t, k in items:
+            worst = max(worst, np.abs(q[k] - X[t]).max())
+    assert worst < 1e-8, worst
+
+
+def test_c2h_soap_gradients(golden):
+    ref = np.load(os.path.join(golden, "c2h_soap_grad.npz"))
+    pos = np.array([[0., 0., 0.], [0.875, 0.875, 0.875], [0.2, 0.2, 0.1]])
+    cell = np.array([[0.0, 1.75, 1.75], [1.75, 0.0, 1.75], [1.75, 1.75, 0.0]])
+    Z = np.array([6, 6, 1])
+    # quippy's Descriptor.calc builds the connection with cutoff = descriptor cutoff + 1
+    q, g, gi = oracle.soap("soap cutoff=1.3 l_max=4 n_max=4 atom_sigma=0.5 n_Z=2 Z={1 6}", pos, Z, cell.T, [1, 1, 1],
+                           grad=True, list_cutoff=2.3)
+    assert q.shape == (3, 51)
+    assert g.shape == (7, 3, 51)
+    np.testing.assert_array_equal(gi, ref["grad_index"])
+    assert np.abs(g[:2] - ref["grad"]).max() < 1e-7
+
+
+def _water():
+    return read_xyz(os.path.join(os.path.dirname(__file__), "golden", "gap_water", "gap_sample.xyz"))[0]
+
+
+def test_gap_distance_2b_energy_forces(golden):
+    at = _water()
+    m = oracle.OracleModel.from_xml(os.path.join(golden, "gap_water", "GAP.xml"))
+    r = m.calc(at.positions, at.numbers, at.lattice, [1, 1, 1])
+    assert abs(r["energy"] - at.info["energy"]) < 1e-5
+    assert np.abs(r["force"] - at.arrays["force"]).max() < 1e-6
+    # tighter than the reference test: FP64 restatement of the same arithmetic
+    assert abs(r["energy"] - at.info["energy"]) < 1e-7
+
+
+def test_potential_cell_energies(golden):
+    d = json.load(open(os.path.join(golden, "potential_cell.json")))
+    m = oracle.OracleModel.from_xml(os.path.join(golden, "gap_water", "GAP.xml"))
+    es = []
+    for c in d["cell_sizes"]:
+        r = m.calc(np.array(d["positions"]), [1, 1], np.eye(3) * c, [1, 1, 1])
+        es.append(r["energy"])
+    assert np.abs(np.array(es) - np.array(d["ref_energies"])).max() < d["tol"]
+
+
+def test_oracle_forces_are_energy_gradient(golden):
+    """Finite differences of E reproduce F and the virial (pot_test_gradient analogue,
+    src/Potentials/Potential.f95:1374-1444)."""
+    frames = read_xyz(os.path.join(golden, "Si.np1.xyz"))
+    fr = frames[4]  # 16-atom periodic Si cell
+    ref = np.load(os.path.join(golden, "si_soap_cur_points.npz"))
+    X = ref["sparsex"]
+    rng = np.random.default_rng(0)
+    parsed = dict(e0={14: -0.5}, coords=[dict(desc_str=SI_SOAP, desc=oracle.parse_args(SI_SOAP), cov=2, delta=3.0, zeta=4.0,
+                                              theta=None, M=100, D=325, X=X, alpha=rng.normal(0, 1, 100), sc=np.ones(100))])
+    m = oracle.OracleModel(parsed)
+    r = m.calc(fr.positions, fr.numbers, fr.lattice)
+    h = 1e-5
+    for a, k in [(0, 0), (3, 1), (7, 2)]:
+        p1 = fr.positions.copy(); p1[a, k] += h
+        p2 = fr.positions.copy(); p2[a, k] -= h
+        fd = -(m.calc(p1, fr.numbers, fr.lattice)["energy"] - m.calc(p2, fr.numbers, fr.lattice)["energy"]) / (2 * h)
+        assert abs(fd - r["force"][a, k]) < 1e-6
+    # virial = -dE/d(strain) for a homogeneous deformation
+    for a, b in [(0, 0), (0, 1), (2, 1)]:
+        eps = np.zeros((3, 3)); eps[a, b] = h
+        e1 = m.calc(fr.positions @ (np.eye(3) + eps).T, fr.numbers, (np.eye(3) + eps) @ fr.lattice)["energy"]
+        e2 = m.calc(fr.positions @ (np.eye(3) - eps).T, fr.numbers, (np.eye(3) - eps) @ fr.lattice)["energy"]
+        assert abs(-(e1 - e2) / (2 * h) - r["virial"][a, b]) < 1e-5
+    np.testing.assert_allclose(r["local_virial"].sum(0), r["virial"], atol=1e-10)
+    np.testing.assert_allclose(r["local_energy"].sum(), r["energy"], atol=1e-10)
