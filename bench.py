@@ -1,0 +1,325 @@
+"""GAP-SOAP energy+force+virial throughput on one GB300 (atom-evals/s).
+
+One "step" is one full evaluation (neighbour list, SOAP and gradients, sparse-GP
+kernel GEMMs, forces, virial) of one structure of the chosen workload:
+  si4096   4096-atom Si diamond 8x8x8 (a=5.43 A, rattle N(0, 0.1 A)); SOAP n_max=8
+           l_max=6 rc=5 A (D=253), 2000 sparse points, zeta=4, + distance_2b (20 points).
+  sic32768 32768-atom random Si/C cell (50/50, 3.2 g/cm^3, 1.6 A minimum separation);
+           SOAP n_max=10 l_max=8 rc=5 A with 2 species channels (D=1891), 8000 sparse
+           points, zeta=4, + distance_2b per species pair.
+Inputs are seeded synthetic structures and random GAP models (no dataset is published
+for this path).  `value` is timed with CUDA events on the launching stream with the
+inputs resident in HBM; `e2e` goes through the public C ABI (gapgpu_calc) with pinned
+host buffers, host<->device copies inside the timed region.  L2 is flushed (256 MB
+write) between timed steps.  `--impl reference` times the FP64 CPU restatement of the
+reference (oracle/) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GAP-SOAP atom-evals/s E+F, mixed vs FP64 on GB300 at <=1 meV/A; p50/p99 latency"
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "fallback": True}
+
+
+WORKLOADS = {
+    "si4096": dict(kind="si", n_rep=8, rattle=0.1, n_max=8, l_max=6, cutoff=5.0, M=2000, species=(14,), seed=11),
+    "si64": dict(kind="si", n_rep=2, rattle=0.05, n_max=8, l_max=6, cutoff=5.0, M=500, species=(14,), seed=7),
+    "sic32768": dict(kind="sic", n=32768, n_max=10, l_max=8, cutoff=5.0, M=8000, species=(14, 6), seed=21),
+}
+
+
+def make_structure(w):
+    from quip_gb300 import models
+    if w["kind"] == "si":
+        return models.si_diamond(w["n_rep"], rattle=w["rattle"], seed=w["seed"])
+    return models.random_binary(w["n"], seed=w["seed"])
+
+
+def make_model(w, tmpdir, descriptor_fn):
+    from quip_gb300 import models
+    if w["kind"] == "si":
+        structs = [models.si_diamond(4, rattle=0.05 + 0.03 * k, seed=200 + k) for k in range(max(1, w["M"] // 512 + 1))]
+    else:
+        structs = [models.random_binary(2048, seed=300 + k) for k in range(w["M"] // 2048 + 1)]
+    return models.random_soap_gap(os.path.join(tmpdir, "bench_gap.xml"), descriptor_fn, structs, n_max=w["n_max"],
+                                  l_max=w["l_max"], cutoff=w["cutoff"], width=1.0, atom_sigma=0.5,
+                                  species=w["species"], M=w["M"], zeta=4.0, delta=1.0, seed=w["seed"])
+
+
+def algorithmic_flops(w, nu):
+    """Per-atom FLOPs of one evaluation (canonical count): expansion, power spectrum,
+    kernel + weight GEMMs, adjoint to c, force contraction."""
+    n, L = w["n_max"], w["l_max"] + 1
+    N = n * len(w["species"])
+    P = N * (N + 1) // 2
+    D = P * L + 1
+    M = w["M"]
+    gemm = 2 * (2 * D * M)
+    return 2 * (nu * n * L * L + P * L * L + N * N * L * L + 3 * nu * n * L * L) + gemm, gemm
+
+
+class Clocks:
+    def __init__(self, path):
+        self.path = path
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+            rows = [r for r in rows if r[0].strip() == rows[0][0].strip()]
+            sm = [float(r[1]) for r in rows]
+            mx = max(float(r[2]) for r in rows)
+            reasons = set()
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for r in rows:
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip() == "Active":
+                        reasons.add(nm)
+            return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(rows)}
+        except Exception as e:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "error": str(e)[:80]}
+
+
+def cpu_reference(w, at, model_path, steps, warmup, sample_atoms=None):
+    """Times the FP64 CPU restatement (oracle) on the host cores."""
+    from oracle import oracle
+    om = oracle.OracleModel.from_xml(model_path)
+    n = len(at)
+    mask = None
+    ncent = n
+    if sample_atoms and sample_atoms < n:
+        mask = np.zeros(n, np.int32)
+        mask[np.random.default_rng(0).choice(n, sample_atoms, replace=False)] = 1
+        ncent = sample_atoms
+    cores = os.cpu_count()
+    for _ in range(warmup):
+        om.calc(at.positions, at.numbers, at.lattice, [1, 1, 1], mask=mask, nthreads=cores)
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        om.calc(at.positions, at.numbers, at.lattice, [1, 1, 1], mask=mask, nthreads=cores)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.median(ts))
+    return {"value": ncent / t, "unit": "atom-evals/s", "cores": cores, "kind": "port",
+            "sample": "%d of %d centres of the %s workload, median of %d" % (ncent, n, w["name"], steps),
+            "seconds_per_sample": t}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="si4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "bf16x3", "tf32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    w = dict(WORKLOADS[args.workload], name=args.workload)
+    warmup = max(3, args.warmup)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        from oracle import oracle
+
+        def oracle_descriptor_fn(desc, a):
+            return oracle.soap(desc, a.positions, a.numbers, a.lattice, a.pbc)
+
+        tmp = tempfile.mkdtemp(prefix="gapref")
+        at = make_structure(w)
+        path = make_model(w, tmp, oracle_descriptor_fn)
+        sample = None if len(at) * w["M"] * w["n_max"] <= 4096 * 2000 * 8 else 256
+        cb = cpu_reference(w, at, path, args.steps, 1, sample)
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "atom-evals/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 * cb["seconds_per_sample"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded structures, random GAP model)",
+                "config": {"workload": args.workload, "precision": "fp64", "atoms": len(at), "sparse_points": w["M"]},
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": "atom-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    from quip_gb300 import _lib, models
+    from quip_gb300.potential import Potential
+
+    tmp = tempfile.mkdtemp(prefix="gapbench")
+    at = make_structure(w)
+    path = make_model(w, tmp, models.bootstrap_descriptor_fn("fp64"))
+    n = len(at)
+    pot = Potential(param_filename=path, precision=args.precision)
+    L = pot._L
+    stream = torch.cuda.current_stream()
+    _lib.check(L.gapgpu_context_set_stream(pot._ctx, _lib.ctypes.c_void_p(stream.cuda_stream)))
+    d_pos = torch.tensor(at.positions, dtype=torch.float64, device="cuda").contiguous()
+    d_Z = torch.tensor(at.numbers, dtype=torch.int32, device="cuda")
+    d_E = torch.zeros(1, dtype=torch.float64, device="cuda")
+    d_F = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
+    d_V = torch.zeros(9, dtype=torch.float64, device="cuda")
+    lat = np.asfortranarray(at.lattice).ravel(order="F").copy()
+    pbc = np.ones(3, np.int32)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        _lib.check(L.gapgpu_calc_device(pot._ctx, n, d_pos.data_ptr(), d_Z.data_ptr(), _lib.ptr(lat), _lib.ptr(pbc),
+                                        d_E.data_ptr(), d_F.data_ptr(), d_V.data_ptr()))
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stage = np.zeros(7)
+    launches = 0
+    clk = Clocks(os.path.join(tmp, "clocks.csv"))
+    with clk:
+        t_wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            step()
+            evs[k][1].record(stream)
+            stage += np.array(list(pot.timings().values()))
+            launches += pot.launches()
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    ms = [a.elapsed_time(b) for a, b in evs]
+    t_dev = sum(ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = world * n * args.steps / t_dev
+    stage /= args.steps
+
+    # end to end through the public host API with pinned buffers
+    pin_pos = torch.tensor(at.positions, dtype=torch.float64).pin_memory()
+    pin_Z = torch.tensor(at.numbers, dtype=torch.int32).pin_memory()
+    pin_F = torch.zeros((n, 3), dtype=torch.float64).pin_memory()
+    pin_V = torch.zeros(9, dtype=torch.float64).pin_memory()
+    pin_E = torch.zeros(1, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        _lib.check(L.gapgpu_calc(pot._ctx, n, pin_pos.data_ptr(), pin_Z.data_ptr(), _lib.ptr(lat), _lib.ptr(pbc), None,
+                                 pin_E.data_ptr(), None, pin_F.data_ptr(), pin_V.data_ptr(), None, b""))
+
+    for _ in range(2):
+        e2e_step()
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_value = n * args.steps / (sum(e2e_ms) / 1e3)
+
+    # neighbour statistics for the algorithmic count
+    off, j, sh = pot.neighbours(at, w["cutoff"])
+    d = at.positions[j] - np.repeat(at.positions, np.diff(off), axis=0) + (at.lattice @ sh.T).T
+    nu = float(np.sum(np.linalg.norm(d, axis=1) < w["cutoff"])) / n
+    flops_atom, gemm_atom = algorithmic_flops(w, nu)
+    pk = peaks()
+    gemm_ms = stage[2]
+    gemm_tflops = n * gemm_atom / (gemm_ms / 1e3) / 1e12 if gemm_ms > 0 else None
+    if args.precision == "fp64":
+        # FP64 reference peak: cuBLAS DGEMM through torch (measured now, 4096^3)
+        a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            a @ b
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        peak = 5 * 2 * 4096 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
+        bound, punit, pnote = "fp64", "TFLOP/s", "cuBLAS DGEMM 4096^3 measured in this run"
+        del a, b
+    else:
+        peak = pk["bf16_tflops"] / (3.0 if args.precision == "bf16x3" else 2.0)
+        bound, punit, pnote = "tensor", "TFLOP/s", "measured bf16 burst / %s" % ("3 (split-BF16 products)" if args.precision == "bf16x3" else "2 (TF32 rate)")
+    roofline = {"bound": bound, "kernel": "sparse-GP kernel GEMMs (K = Q X^T, G = W X)", "achieved": gemm_tflops,
+                "peak": peak, "unit": punit, "frac": (gemm_tflops / peak) if gemm_tflops else None, "traffic": None,
+                "peak_source": pnote, "gemm_flops_per_atom": gemm_atom}
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        sample = None if n * w["M"] <= 4096 * 2000 else 256
+        try:
+            cb = cpu_reference(w, at, path, 1, 0, sample)
+            cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as e:
+            cpu = {"value": None, "error": str(e)[:120]}
+
+    if rank == 0:
+        h2d = n * 3 * 8 + n * 4
+        d2h = 8 + n * 3 * 8 + 9 * 8
+        line = {"metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": world, "steps": args.steps,
+                "warmup": warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+" + args.precision,
+                "data": "synthetic: seeded structures and a random GAP model (no published dataset for this path)",
+                "config": {"workload": args.workload, "precision": args.precision, "atoms": n, "sparse_points": w["M"],
+                           "soap": "n_max=%d l_max=%d rc=%g species=%s" % (w["n_max"], w["l_max"], w["cutoff"],
+                                                                           list(w["species"])),
+                           "mean_neighbours": nu, "l2": "256 MB flush between timed steps",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "stage_ms": dict(zip(["neighbours", "soap_fwd", "gemm", "soap_bwd", "pair2b", "reduce", "total"],
+                                     [round(x, 4) for x in stage])),
+                "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": {"value": e2e_value, "unit": "atom-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
+                "gpu_launches": int(launches), "clocks": clk.summary(),
+                "algorithmic_flops_per_atom": flops_atom, "wall_s": t_wall}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,131 @@
+/* gapgpu.h -- C ABI of the GB300 GAP energy/force/virial library (libgapgpu.so).
+ *
+ * The library replaces the body of QUIP's IPModel_GAP_Calc
+ * (src/Potentials/IPModel_GAP.f95:233-605) and the connection build it relies on
+ * (connection_calc_connect, src/libAtoms/Connection.f95:1035-1310).  Everything above
+ * it -- potential_calc (src/Potentials/Potential.f95:803-996), quippy's
+ * Potential.calculate (quippy/quippy/potential.py:177-325), DynamicalSystem MD -- keeps
+ * its signatures; a Fortran iso_c_binding module binds these symbols.
+ *
+ * Conventions (all match QUIP's Fortran arrays, so no copies are needed there):
+ *   pos           double[3*n]   Fortran pos(3,N): pos[3*i + k]
+ *   Z             int32[n]
+ *   lattice       double[9]     Fortran lattice(3,3), COLUMNS are the cell vectors:
+ *                               lattice[3*c + k] = component k of cell vector c
+ *   pbc           int32[3]      at%is_periodic
+ *   force         double[3*n]   Fortran f(3,N)
+ *   virial        double[9]     Fortran virial(3,3), column-major
+ *   local_virial  double[9*n]   Fortran local_virial(9,N) = reshape(virial_i, (/9/))
+ * Any output pointer may be NULL (the Fortran `present()` test).
+ *
+ * Errors: every entry point returns 0 (GAPGPU_OK) or a positive error kind and never
+ * aborts; gapgpu_last_error() gives the message of the calling thread's last failure
+ * (the Fortran shim maps it to RAISE_ERROR, src/libAtoms/error.inc:61).
+ *
+ * Threading: one calculation at a time per context.  A model may be shared by several
+ * contexts (one per CUDA stream) once created.  There is no CPU fallback: without a
+ * usable sm_103a GPU every compute entry point returns GAPGPU_ERR_CUDA.
+ */
+#ifndef GAPGPU_H
+#define GAPGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gapgpu_model gapgpu_model;
+typedef struct gapgpu_context gapgpu_context;
+
+enum gapgpu_status {
+    GAPGPU_OK = 0,
+    GAPGPU_ERR_ARG = 1,          /* bad argument (NULL handle, size mismatch, unknown args_str key) */
+    GAPGPU_ERR_XML = 2,          /* GAP XML could not be read or is inconsistent */
+    GAPGPU_ERR_UNSUPPORTED = 3,  /* model feature outside this library (descriptor type, covariance) */
+    GAPGPU_ERR_CUDA = 4,         /* no usable GPU, or a CUDA call failed */
+    GAPGPU_ERR_ATOMS = 5,        /* atoms rejected: negative cutoff, overlapping atoms, NaN positions */
+    GAPGPU_ERR_TIMEOUT = 6       /* a bounded device-side wait gave up */
+};
+
+enum gapgpu_precision {
+    GAPGPU_FP64 = 0,       /* plain path: every stage in FP64 */
+    GAPGPU_MIXED_BF16X3 = 1, /* SOAP in FP32, kernel GEMMs as split-BF16 (hi*hi + hi*lo + lo*hi) on tcgen05 */
+    GAPGPU_MIXED_TF32 = 2  /* SOAP in FP32, kernel GEMMs in TF32 on tcgen05 */
+};
+
+/* Message of the calling thread's last error ("" if none). */
+const char* gapgpu_last_error(void);
+
+/* Build a model from GAP XML text.  Replaces potential_Filename_Initialise
+ * (src/Potentials/Potential.f95:438-468) + IPModel_GAP_Initialise_str
+ * (src/Potentials/IPModel_GAP.f95:149-192): `label` selects the GAP_params stanza
+ * (NULL/"" = first), sparseX_filename entries are resolved relative to `base_dir`
+ * (the reference changes into the XML file's directory, Potential.f95:455-466).
+ * `init_args` is the reference's init args_str (keys: label, E_scale). */
+int gapgpu_model_create(const char* xml, size_t xml_len, const char* init_args, const char* base_dir,
+                        gapgpu_model** out);
+
+/* Potential cutoff = max descriptor cutoff (IPModel_GAP.f95:182-188). */
+int gapgpu_model_cutoff(const gapgpu_model* model, double* cutoff);
+
+/* Descriptor dimensions and sparse-point counts, for diagnostics and the autotuner. */
+int gapgpu_model_info(const gapgpu_model* model, int* n_coordinates, int* dims, int* n_sparse, int capacity);
+
+void gapgpu_model_destroy(gapgpu_model* model);
+
+/* Per-stream evaluation context that owns the device workspace (neighbour lists,
+ * descriptors, GEMM operands) and keeps it between calls. */
+int gapgpu_context_create(const gapgpu_model* model, int precision, gapgpu_context** out);
+int gapgpu_context_set_stream(gapgpu_context* ctx, void* cuda_stream);
+void gapgpu_context_destroy(gapgpu_context* ctx);
+
+/* The drop-in calculation: IPModel_GAP_Calc(this, at, e, local_e, f, virial,
+ * local_virial, args_str) (IPModel_GAP.f95:233-241) with the connection built inside
+ * (Potential.f95:844-858).  Host arrays in, host arrays out.  `atom_mask` (nullable)
+ * is the logical property named by args_str atom_mask_name: it restricts the
+ * centres (and the e0 sum) exactly as the reference does.  Recognised args keys:
+ * atom_mask_name (value ignored here: pass the mask array), r_scale / E_scale
+ * (rejected, as in IPModel_GAP.f95:348-350), xml_version, precision=fp64|bf16x3|tf32.
+ * Unknown keys are ignored, like param_read_line(ignore_unknown=.true.). */
+int gapgpu_calc(gapgpu_context* ctx, int n, const double* pos, const int32_t* Z, const double* lattice,
+                const int32_t* pbc, const int32_t* atom_mask, double* energy, double* local_e, double* force,
+                double* virial, double* local_virial, const char* args);
+
+/* Same calculation with device-resident inputs and outputs on the context's stream
+ * (no host synchronisation).  d_pos double[3n], d_Z int32[n]; lattice and pbc stay on
+ * the host.  Outputs are device pointers (nullable).  Used by batching, serving and
+ * device-resident MD, which keep positions in HBM between steps. */
+int gapgpu_calc_device(gapgpu_context* ctx, int n, const double* d_pos, const int32_t* d_Z, const double* lattice,
+                       const int32_t* pbc, double* d_energy, double* d_force, double* d_virial);
+
+/* Wait for the context's stream. */
+int gapgpu_context_sync(gapgpu_context* ctx);
+
+/* Neighbour list with QUIP semantics (no minimum image, every periodic image within
+ * `cutoff`, strict r < cutoff) built on the GPU: connection_calc_connect
+ * (Connection.f95:1035-1310).  Returns per-atom CSR (offsets n+1, j, shift 3 per
+ * entry); when `capacity` is too small only offsets/total are filled.  Order within an
+ * atom's list is deterministic but not the reference's linked-list order. */
+int gapgpu_neighbours(gapgpu_context* ctx, int n, const double* pos, const double* lattice, const int32_t* pbc,
+                      double cutoff, int32_t* offsets, int32_t* nbr_j, int32_t* nbr_shift, int64_t capacity,
+                      int64_t* total);
+
+/* SOAP descriptors (and the sum of squares before normalisation) of every centre
+ * for coordinate `coordinate` of the model: the descriptor-only path of
+ * quippy/quippy/descriptors.py:165-235.  q: n_centres*dim row-major. */
+int gapgpu_descriptors(gapgpu_context* ctx, int coordinate, int n, const double* pos, const int32_t* Z,
+                       const double* lattice, const int32_t* pbc, double* q, int64_t capacity, int* n_centres);
+
+/* Last calculation's stage timings in ms (CUDA events): neighbours, soap_fwd, gemm,
+ * soap_bwd, pair2b, reduce, total.  Returns the number of entries written. */
+int gapgpu_context_timings(const gapgpu_context* ctx, double* ms, int capacity);
+
+/* Number of this library's kernel launches issued by the last calculation. */
+int gapgpu_context_launches(const gapgpu_context* ctx, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GAPGPU_H */

@@ -1,0 +1,78 @@
+"""ctypes binding of libgapgpu.so (include/gapgpu.h).
+
+The library is the product: there is no Python or CPU compute path behind these
+bindings.  If the shared library is missing it is built; if no GPU is usable every
+compute entry point returns GAPGPU_ERR_CUDA and the Python side raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgapgpu.so")
+
+OK, ERR_ARG, ERR_XML, ERR_UNSUPPORTED, ERR_CUDA, ERR_ATOMS, ERR_TIMEOUT = range(7)
+FP64, MIXED_BF16X3, MIXED_TF32 = 0, 1, 2
+PRECISIONS = {"fp64": FP64, "bf16x3": MIXED_BF16X3, "tf32": MIXED_TF32}
+
+# Every symbol declared in include/gapgpu.h.
+EXPORTS = ["gapgpu_last_error", "gapgpu_model_create", "gapgpu_model_cutoff", "gapgpu_model_info",
+           "gapgpu_model_destroy", "gapgpu_context_create", "gapgpu_context_set_stream", "gapgpu_context_destroy",
+           "gapgpu_calc", "gapgpu_calc_device", "gapgpu_context_sync", "gapgpu_neighbours", "gapgpu_descriptors",
+           "gapgpu_context_timings", "gapgpu_context_launches"]
+
+
+class GapGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gapgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise OSError("libgapgpu.so is not built")
+        from . import build
+        build.build()
+    L = ctypes.CDLL(LIB_PATH)
+    c_int, c_double, c_size_t, c_char_p, c_void_p = ctypes.c_int, ctypes.c_double, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_void_p
+    P = ctypes.POINTER
+    i64 = ctypes.c_int64
+    L.gapgpu_last_error.restype = c_char_p
+    L.gapgpu_model_create.argtypes = [c_char_p, c_size_t, c_char_p, c_char_p, P(c_void_p)]
+    L.gapgpu_model_cutoff.argtypes = [c_void_p, P(c_double)]
+    L.gapgpu_model_info.argtypes = [c_void_p, P(c_int), P(c_int), P(c_int), c_int]
+    L.gapgpu_model_destroy.argtypes = [c_void_p]
+    L.gapgpu_model_destroy.restype = None
+    L.gapgpu_context_create.argtypes = [c_void_p, c_int, P(c_void_p)]
+    L.gapgpu_context_set_stream.argtypes = [c_void_p, c_void_p]
+    L.gapgpu_context_destroy.argtypes = [c_void_p]
+    L.gapgpu_context_destroy.restype = None
+    L.gapgpu_context_sync.argtypes = [c_void_p]
+    L.gapgpu_calc.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                              c_void_p, c_void_p, c_void_p, c_char_p]
+    L.gapgpu_calc_device.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                     c_void_p]
+    L.gapgpu_neighbours.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
+                                    c_void_p, i64, P(i64)]
+    L.gapgpu_descriptors.argtypes = [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, i64,
+                                     P(c_int)]
+    L.gapgpu_context_timings.argtypes = [c_void_p, P(c_double), c_int]
+    L.gapgpu_context_launches.argtypes = [c_void_p, P(i64)]
+    _lib = L
+    return L
+
+
+def check(code):
+    if code != OK:
+        raise GapGpuError(code, load().gapgpu_last_error().decode())
+
+
+def ptr(a):
+    """Raw data pointer of a numpy array (or None)."""
+    return None if a is None else a.ctypes.data

@@ -1,0 +1,354 @@
+// neighbours.cu -- K1: cell-list neighbour build with QUIP's semantics.
+//
+// Restates connection_calc_connect (src/libAtoms/Connection.f95:1035-1310) for the GPU:
+//   * atoms are wrapped into the (effective) cell by map_shift = -floor(s + 0.5)
+//     (partition_atoms :1519-1587) and binned with cell_of_pos (:1589-1621);
+//   * cells per axis from divide_cell (:1674-1691), image range per axis from
+//     fit_box_in_cell (:2204-2237) reduced to max(1, (N+1)/2) (:1145-1151), clipped
+//     for non-periodic axes as get_min_max_images (:1448-1513);
+//   * a pair (i, j, shift) is kept when |r_j + L shift - r_i| < cutoff (strict,
+//     test_form_bond :517); there is NO minimum-image convention, every periodic image
+//     inside the cutoff is its own entry, and only the exact self at zero shift in the
+//     same cell is skipped (:1265-1270);
+//   * pair shift = cell-image shift - map_shift_i + map_shift_j (:1273-1276).
+// The reference builds a half list (atom1 <= atom2) and exposes both directions
+// through neighbour1/neighbour2.  The image ranges are symmetric, so every atom's
+// full list is exactly the set the reference iterates; here each atom scans its own
+// image cells and emits its full list directly (no atomics: count, scan, fill).
+// Atoms are sorted by cell with a stable radix sort so that each list has a fixed,
+// reproducible order (cell-image loop order, then atom index).
+#include <cub/cub.cuh>
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+
+#include "context.h"
+
+namespace gapgpu {
+
+namespace {
+
+__device__ __forceinline__ int pack_shift(int a, int b, int c) {
+    return ((a + 512) & 1023) | (((b + 512) & 1023) << 10) | (((c + 512) & 1023) << 20);
+}
+
+struct GeomDev {
+    double lat[9], lat_eff_inv[9], lat_off[3], cutoff;
+    int cellsN[3], img[3], pbc[3];
+};
+
+__global__ void k_assign(int n, const double* __restrict__ pos, GeomDev g, int* __restrict__ key, int* __restrict__ idx,
+                         int* __restrict__ ms, int* __restrict__ bad) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    double p[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+    if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) atomicOr(bad, 1);
+    int c3[3];
+    for (int d = 0; d < 3; ++d) {
+        double lp = g.lat_eff_inv[d] * p[0] + g.lat_eff_inv[3 + d] * p[1] + g.lat_eff_inv[6 + d] * p[2] - g.lat_off[d];
+        int m = g.pbc[d] ? -(int)floor(lp + 0.5) : 0;
+        ms[3 * a + d] = m;
+        double t = lp + m;
+        int ci = (int)floor((double)g.cellsN[d] * (t + 0.5)) + 1;
+        ci = ci < 1 ? 1 : (ci > g.cellsN[d] ? g.cellsN[d] : ci);
+        c3[d] = ci - 1;
+    }
+    key[a] = c3[0] + g.cellsN[0] * (c3[1] + g.cellsN[1] * c3[2]);
+    idx[a] = a;
+}
+
+__global__ void k_cell_ranges(int n, const int* __restrict__ key, int* __restrict__ start, int* __restrict__ end) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int c = key[k];
+    if (k == 0 || key[k - 1] != c) start[c] = k;
+    if (k == n - 1 || key[k + 1] != c) end[c] = k + 1;
+}
+
+// Visits every candidate (a2, shift) of atom a in the reference's cell-image order.
+template <class F>
+__device__ void scan_images(int a, const double* __restrict__ pos, const GeomDev& g, const int* __restrict__ key_of_atom,
+                            const int* __restrict__ ms, const int* __restrict__ sorted, const int* __restrict__ cstart,
+                            const int* __restrict__ cend, F&& emit) {
+    int lin = key_of_atom[a];
+    int cc[3] = {lin % g.cellsN[0], (lin / g.cellsN[0]) % g.cellsN[1], lin / (g.cellsN[0] * g.cellsN[1])};
+    int mn[3], mx[3];
+    for (int d = 0; d < 3; ++d) {
+        int c1 = cc[d] + 1;  // 1-based as in the reference
+        if (g.pbc[d]) { mn[d] = -g.img[d]; mx[d] = g.img[d]; }
+        else {
+            mn[d] = (g.img[d] < c1) ? -g.img[d] : -c1 + 1;
+            mx[d] = (g.img[d] < g.cellsN[d] - c1) ? g.img[d] : g.cellsN[d] - c1;
+        }
+    }
+    const double pa0 = pos[3 * a], pa1 = pos[3 * a + 1], pa2 = pos[3 * a + 2];
+    const int msa0 = ms[3 * a], msa1 = ms[3 * a + 1], msa2 = ms[3 * a + 2];
+    for (int k2 = mn[2]; k2 <= mx[2]; ++k2) {
+        int k3 = 0, k4;
+        int t = cc[2] + k2;
+        if (g.cellsN[2] > 1) k3 = ((t % g.cellsN[2]) + g.cellsN[2]) % g.cellsN[2];
+        k4 = (t - k3) / g.cellsN[2];
+        for (int j2 = mn[1]; j2 <= mx[1]; ++j2) {
+            int j3 = 0, j4;
+            int u = cc[1] + j2;
+            if (g.cellsN[1] > 1) j3 = ((u % g.cellsN[1]) + g.cellsN[1]) % g.cellsN[1];
+            j4 = (u - j3) / g.cellsN[1];
+            for (int i2 = mn[0]; i2 <= mx[0]; ++i2) {
+                int i3 = 0, i4;
+                int v = cc[0] + i2;
+                if (g.cellsN[0] > 1) i3 = ((v % g.cellsN[0]) + g.cellsN[0]) % g.cellsN[0];
+                i4 = (v - i3) / g.cellsN[0];
+                int cl = i3 + g.cellsN[0] * (j3 + g.cellsN[1] * k3);
+                bool same_cell = (cl == lin);
+                int e = cend[cl];
+                for (int q = cstart[cl]; q < e; ++q) {
+                    int b = sorted[q];
+                    if (b == a && i4 == 0 && j4 == 0 && k4 == 0 && same_cell) continue;
+                    int s0 = i4 - msa0 + ms[3 * b], s1 = j4 - msa1 + ms[3 * b + 1], s2 = k4 - msa2 + ms[3 * b + 2];
+                    // dd = pos_b - pos_a + lattice . shift, accumulated column by column
+                    // without fused multiply-adds, as test_form_bond does
+                    double d0 = __dsub_rn(pos[3 * b], pa0), d1 = __dsub_rn(pos[3 * b + 1], pa1), d2 = __dsub_rn(pos[3 * b + 2], pa2);
+                    d0 = __dadd_rn(d0, __dmul_rn(g.lat[0], (double)s0)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[1], (double)s0));
+                    d2 = __dadd_rn(d2, __dmul_rn(g.lat[2], (double)s0));
+                    d0 = __dadd_rn(d0, __dmul_rn(g.lat[3], (double)s1)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[4], (double)s1));
+                    d2 = __dadd_rn(d2, __dmul_rn(g.lat[5], (double)s1));
+                    d0 = __dadd_rn(d0, __dmul_rn(g.lat[6], (double)s2)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[7], (double)s2));
+                    d2 = __dadd_rn(d2, __dmul_rn(g.lat[8], (double)s2));
+                    if (d0 > g.cutoff || d1 > g.cutoff || d2 > g.cutoff) continue;
+                    double r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+                    if (r < g.cutoff) emit(b, s0, s1, s2, d0, d1, d2, r);
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_count(int n, const double* __restrict__ pos, GeomDev g, const int* __restrict__ key_of_atom,
+                        const int* __restrict__ ms, const int* __restrict__ sorted, const int* __restrict__ cstart,
+                        const int* __restrict__ cend, int* __restrict__ cnt) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    int c = 0;
+    scan_images(a, pos, g, key_of_atom, ms, sorted, cstart, cend,
+                [&](int, int, int, int, double, double, double, double) { ++c; });
+    cnt[a] = c;
+}
+
+__global__ void k_fill(int n, const double* __restrict__ pos, GeomDev g, const int* __restrict__ key_of_atom,
+                       const int* __restrict__ ms, const int* __restrict__ sorted, const int* __restrict__ cstart,
+                       const int* __restrict__ cend, const int* __restrict__ off, int* __restrict__ nj,
+                       double4* __restrict__ nd, int* __restrict__ ns, int* __restrict__ bad) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    int p = off[a];
+    scan_images(a, pos, g, key_of_atom, ms, sorted, cstart, cend,
+                [&](int b, int s0, int s1, int s2, double d0, double d1, double d2, double r) {
+                    nj[p] = b;
+                    nd[p] = make_double4(d0, d1, d2, r);
+                    ns[p] = pack_shift(s0, s1, s2);
+                    if (r < 1e-10) atomicOr(bad, 2);
+                    ++p;
+                });
+}
+
+__global__ void k_reverse(int n, const int* __restrict__ off, const int* __restrict__ nj, const int* __restrict__ ns,
+                          int* __restrict__ rev, int* __restrict__ bad) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    for (int p = off[a]; p < off[a + 1]; ++p) {
+        int b = nj[p];
+        int s = ns[p];
+        int s0 = (s & 1023) - 512, s1 = ((s >> 10) & 1023) - 512, s2 = ((s >> 20) & 1023) - 512;
+        int want = pack_shift(-s0, -s1, -s2);
+        int found = -1;
+        for (int q = off[b]; q < off[b + 1]; ++q)
+            if (nj[q] == a && ns[q] == want) { found = q; break; }
+        rev[p] = found;
+        if (found < 0) atomicOr(bad, 4);
+    }
+}
+
+void inv3(const double* a, double* g) {
+    auto A = [&](int r, int c) { return a[3 * c + r]; };
+    double det = A(0, 0) * (A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) - A(0, 1) * (A(1, 0) * A(2, 2) - A(1, 2) * A(2, 0)) +
+                 A(0, 2) * (A(1, 0) * A(2, 1) - A(1, 1) * A(2, 0));
+    double inv[3][3] = {{(A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) / det, (A(0, 2) * A(2, 1) - A(0, 1) * A(2, 2)) / det,
+                         (A(0, 1) * A(1, 2) - A(0, 2) * A(1, 1)) / det},
+                        {(A(1, 2) * A(2, 0) - A(1, 0) * A(2, 2)) / det, (A(0, 0) * A(2, 2) - A(0, 2) * A(2, 0)) / det,
+                         (A(0, 2) * A(1, 0) - A(0, 0) * A(1, 2)) / det},
+                        {(A(1, 0) * A(2, 1) - A(1, 1) * A(2, 0)) / det, (A(0, 1) * A(2, 0) - A(0, 0) * A(2, 1)) / det,
+                         (A(0, 0) * A(1, 1) - A(0, 1) * A(1, 0)) / det}};
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) g[3 * c + r] = inv[r][c];
+}
+
+double norm3(const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+void cross3(const double* a, const double* b, double* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1]; c[1] = a[2] * b[0] - a[0] * b[2]; c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+__global__ void k_latpos_minmax(int n, const double* __restrict__ pos, GeomDev g, double* __restrict__ out) {
+    // one block: min/max of fractional coordinates per axis (calc_lat_eff)
+    __shared__ double smn[3][256], smx[3][256];
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int a = threadIdx.x; a < n; a += blockDim.x) {
+        for (int d = 0; d < 3; ++d) {
+            double lp = g.lat_eff_inv[d] * pos[3 * a] + g.lat_eff_inv[3 + d] * pos[3 * a + 1] + g.lat_eff_inv[6 + d] * pos[3 * a + 2];
+            mn[d] = fmin(mn[d], lp); mx[d] = fmax(mx[d], lp);
+        }
+    }
+    for (int d = 0; d < 3; ++d) { smn[d][threadIdx.x] = mn[d]; smx[d][threadIdx.x] = mx[d]; }
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int d = 0; d < 3; ++d) {
+                smn[d][threadIdx.x] = fmin(smn[d][threadIdx.x], smn[d][threadIdx.x + s]);
+                smx[d][threadIdx.x] = fmax(smx[d][threadIdx.x], smx[d][threadIdx.x + s]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; ++d) { out[d] = smn[d][0]; out[3 + d] = smx[d][0]; }
+}
+
+}  // namespace
+
+int DBuf::ensure(size_t bytes) {
+    if (bytes <= cap && p) return GAPGPU_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+    GG_CUDA(cudaMalloc(&p, want));
+    cap = want;
+    return GAPGPU_OK;
+}
+void DBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+}
+
+int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double* lattice, const int* pbc, double cutoff,
+                     const int*) {
+    if (!(cutoff >= 0.0)) GG_FAIL(GAPGPU_ERR_ATOMS, "calc_connect: negative cutoff radius");
+    cudaStream_t st = c.stream;
+    GeomDev g;
+    std::memset(&g, 0, sizeof g);
+    std::memcpy(g.lat, lattice, sizeof g.lat);
+    g.cutoff = cutoff;
+    for (int d = 0; d < 3; ++d) g.pbc[d] = pbc[d] ? 1 : 0;
+    double gi[9];
+    inv3(lattice, gi);
+    for (double v : gi) if (!std::isfinite(v)) GG_FAIL(GAPGPU_ERR_ATOMS, "lattice is singular");
+    double lat_eff[9];
+    std::memcpy(lat_eff, lattice, sizeof lat_eff);
+    std::memcpy(g.lat_eff_inv, gi, sizeof gi);
+    int rc;
+    if (!g.pbc[0] || !g.pbc[1] || !g.pbc[2]) {  // calc_lat_eff (Connection.f95:740-763)
+        if ((rc = c.minmax.ensure(6 * sizeof(double)))) return rc;
+        k_latpos_minmax<<<1, 256, 0, st>>>(n, d_pos, g, c.minmax.as<double>());
+        c.launches++;
+        double mm[6];
+        GG_CUDA(cudaMemcpyAsync(mm, c.minmax.p, sizeof mm, cudaMemcpyDeviceToHost, st));
+        GG_CUDA(cudaStreamSynchronize(st));
+        for (int d = 0; d < 3; ++d) {
+            if (g.pbc[d]) continue;
+            if (mm[d] <= 0.5 || mm[3 + d] >= 0.5) {
+                double ext = (mm[3 + d] - mm[d]) * 1.1;
+                double nv = norm3(lattice + 3 * d);
+                for (int k = 0; k < 3; ++k) lat_eff[3 * d + k] = lattice[3 * d + k] / nv * ext;
+                g.lat_off[d] = mm[d] - 0.05;
+            }
+        }
+        inv3(lat_eff, g.lat_eff_inv);
+    }
+    // divide_cell
+    {
+        const double *a = lat_eff, *b = lat_eff + 3, *cc = lat_eff + 6;
+        double bc[3], ca[3], ab[3];
+        cross3(b, cc, bc); cross3(cc, a, ca); cross3(a, b, ab);
+        double vol = std::fabs(a[0] * bc[0] + a[1] * bc[1] + a[2] * bc[2]);
+        double cut = cutoff > 0 ? cutoff : 1.0;
+        g.cellsN[0] = std::max(1, (int)std::min(1e6, vol / (cut * norm3(bc))));
+        g.cellsN[1] = std::max(1, (int)std::min(1e6, vol / (cut * norm3(ca))));
+        g.cellsN[2] = std::max(1, (int)std::min(1e6, vol / (cut * norm3(ab))));
+        // Bound the cell grid by the atom count.  The reference's search is complete
+        // (every pair inside the cutoff is found: cells are at least one cutoff wide
+        // and the image range covers the cutoff sphere), so coarser cells scan a
+        // superset of candidates and the distance test returns the identical set.
+        while ((long long)g.cellsN[0] * g.cellsN[1] * g.cellsN[2] > 4LL * n + 64) {
+            int d = (g.cellsN[0] >= g.cellsN[1] && g.cellsN[0] >= g.cellsN[2]) ? 0 : (g.cellsN[1] >= g.cellsN[2] ? 1 : 2);
+            g.cellsN[d] = std::max(1, g.cellsN[d] / 2);
+        }
+    }
+    // fit_box_in_cell on the true lattice
+    {
+        double mx[3] = {0, 0, 0};
+        for (int k = -1; k <= 1; k += 2)
+            for (int j = -1; j <= 1; j += 2)
+                for (int i = -1; i <= 1; i += 2) {
+                    double v[3] = {i * cutoff, j * cutoff, k * cutoff};
+                    for (int d = 0; d < 3; ++d) mx[d] = std::max(mx[d], std::fabs(gi[d] * v[0] + gi[3 + d] * v[1] + gi[6 + d] * v[2]));
+                }
+        for (int d = 0; d < 3; ++d) {
+            int nn = (int)std::ceil(2.0 * mx[d]);
+            g.img[d] = std::max(1, (nn + 1) / 2);
+        }
+        if ((long long)(2 * g.img[0] + 1) * (2 * g.img[1] + 1) * (2 * g.img[2] + 1) > 2000000LL)
+            GG_FAIL(GAPGPU_ERR_ATOMS, "calc_connect: cutoff is too large for the cell (more than 2e6 periodic images)");
+    }
+    const int ncell = g.cellsN[0] * g.cellsN[1] * g.cellsN[2];
+    if ((rc = c.cell_key.ensure(sizeof(int) * n)) || (rc = c.cell_key2.ensure(sizeof(int) * n)) ||
+        (rc = c.atom_idx.ensure(sizeof(int) * n)) || (rc = c.atom_idx2.ensure(sizeof(int) * n)) ||
+        (rc = c.ms.ensure(sizeof(int) * 3 * n)) || (rc = c.cell_start.ensure(sizeof(int) * ncell)) ||
+        (rc = c.cell_end.ensure(sizeof(int) * ncell)) || (rc = c.nbr_cnt.ensure(sizeof(int) * (n + 1))) ||
+        (rc = c.nbr_off.ensure(sizeof(int) * (n + 1))) || (rc = c.total.ensure(sizeof(int) * 4)))
+        return rc;
+    int* bad = c.total.as<int>() + 2;
+    GG_CUDA(cudaMemsetAsync(c.total.p, 0, sizeof(int) * 4, st));
+    const int TB = 128, nb = (n + TB - 1) / TB;
+    k_assign<<<nb, TB, 0, st>>>(n, d_pos, g, c.cell_key.as<int>(), c.atom_idx.as<int>(), c.ms.as<int>(), bad);
+    // stable sort atoms by cell
+    int endbit = 1;
+    while ((1 << endbit) < ncell && endbit < 31) ++endbit;
+    size_t tmp = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp, c.cell_key.as<int>(), c.cell_key2.as<int>(), c.atom_idx.as<int>(),
+                                    c.atom_idx2.as<int>(), n, 0, endbit, st);
+    size_t tmp2 = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tmp2, c.nbr_cnt.as<int>(), c.nbr_off.as<int>(), n + 1, st);
+    if ((rc = c.cub_tmp.ensure(std::max(tmp, tmp2)))) return rc;
+    GG_CUDA(cub::DeviceRadixSort::SortPairs(c.cub_tmp.p, tmp, c.cell_key.as<int>(), c.cell_key2.as<int>(),
+                                            c.atom_idx.as<int>(), c.atom_idx2.as<int>(), n, 0, endbit, st));
+    GG_CUDA(cudaMemsetAsync(c.cell_start.p, 0, sizeof(int) * ncell, st));
+    GG_CUDA(cudaMemsetAsync(c.cell_end.p, 0, sizeof(int) * ncell, st));
+    k_cell_ranges<<<nb, TB, 0, st>>>(n, c.cell_key2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>());
+    k_count<<<nb, TB, 0, st>>>(n, d_pos, g, c.cell_key.as<int>(), c.ms.as<int>(), c.atom_idx2.as<int>(), c.cell_start.as<int>(),
+                               c.cell_end.as<int>(), c.nbr_cnt.as<int>());
+    GG_CUDA(cudaMemsetAsync(c.nbr_cnt.as<int>() + n, 0, sizeof(int), st));
+    GG_CUDA(cub::DeviceScan::ExclusiveSum(c.cub_tmp.p, tmp2, c.nbr_cnt.as<int>(), c.nbr_off.as<int>(), n + 1, st));
+    int tot = 0;
+    GG_CUDA(cudaMemcpyAsync(&tot, c.nbr_off.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GG_CUDA(cudaStreamSynchronize(st));
+    c.launches += 5;
+    if (tot < 0) GG_FAIL(GAPGPU_ERR_ATOMS, "neighbour list larger than 2^31 entries");
+    c.n_pairs = tot;
+    size_t P = std::max(tot, 1);
+    if ((rc = c.nbr_j.ensure(sizeof(int) * P)) || (rc = c.nbr_d.ensure(sizeof(double4) * P)) ||
+        (rc = c.nbr_s.ensure(sizeof(int) * P)) || (rc = c.nbr_rev.ensure(sizeof(int) * P)))
+        return rc;
+    k_fill<<<nb, TB, 0, st>>>(n, d_pos, g, c.cell_key.as<int>(), c.ms.as<int>(), c.atom_idx2.as<int>(), c.cell_start.as<int>(),
+                              c.cell_end.as<int>(), c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(),
+                              c.nbr_s.as<int>(), bad);
+    k_reverse<<<nb, TB, 0, st>>>(n, c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_s.as<int>(), c.nbr_rev.as<int>(), bad);
+    c.launches += 2;
+    int flags = 0;
+    GG_CUDA(cudaMemcpyAsync(&flags, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GG_CUDA(cudaStreamSynchronize(st));
+    if (flags & 1) GG_FAIL(GAPGPU_ERR_ATOMS, "atom positions contain NaN or Inf");
+    if (flags & 2) GG_FAIL(GAPGPU_ERR_ATOMS, "overlapping atoms: a neighbour distance is below 1e-10 (Connection.f95:1394-1398)");
+    if (flags & 4) GG_FAIL(GAPGPU_ERR_ATOMS, "internal error: neighbour list is not symmetric");
+    return GAPGPU_OK;
+}
+
+}  // namespace gapgpu

@@ -1,0 +1,152 @@
+// pair.cu -- K6 distance_2b + ard_se GP, and K7/K8: deterministic force / virial /
+// energy assembly.
+//
+// distance_2b (GAP descriptors_module, absent; pinned by tests/test_gappot.py): one
+// descriptor per DIRECTED pair (i -> j, r < cutoff, species (Z1,Z2) in either order),
+// value r, covariance_cutoff fc(r), energy split e fc / 2 to i and j.
+// ard_se: e = sum_s alpha_s delta^2 sc_s exp(-(r - x_s)^2 / (2 theta^2)).
+//
+// Assembly (src/Potentials/IPModel_GAP.f95:472-499, :523-596): every descriptor
+// contributes, per directed pair p = (i -> j, d = r_j + L s - r_i), a vector
+// f_p = dE_i / dr_j.  The reference scatters F(j) -= f_p, F(i) += f_p and
+// virial(j) -= d (x) f_p.  Here each atom GATHERS over its own list using the
+// reverse-pair index (the pair j -> i of p is rev[p], with d_rev = -d bitwise), so
+// there are no floating-point atomics and the result is bit-identical run to run:
+//   F_a   = sum_{p in a} (f_p - f_rev(p))
+//   W_a   = sum_{p in a} d_p (x) f_rev(p)
+//   e_a   = eatom_a + sum_{p in a} (epair_p + epair_rev(p)) + e0(Z_a) [mask]
+#include "context.h"
+
+namespace gapgpu {
+namespace {
+
+__device__ __forceinline__ void fcut(double r, double rc, double w, double& f, double& df) {
+    if (r > rc) { f = 0; df = 0; return; }
+    if (r > rc - w) {
+        const double pi = 3.14159265358979323846;
+        double a = pi * (r - rc + w) / w;
+        f = 0.5 * (cos(a) + 1.0);
+        df = -0.5 * pi * sin(a) / w;
+        return;
+    }
+    f = 1; df = 0;
+}
+
+__global__ void k_pair_2b(int n, const int* __restrict__ Z, const int* __restrict__ mask, const int* __restrict__ off,
+                          const int* __restrict__ nj, const double4* __restrict__ nd, double rc, double w, int Z1, int Z2,
+                          int M, const double* __restrict__ X, const double* __restrict__ coef, double theta,
+                          double* __restrict__ fpair, double* __restrict__ epair) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    if (mask && !mask[a]) return;
+    const int za = Z[a];
+    const double it2 = 1.0 / (theta * theta);
+    for (int p = off[a]; p < off[a + 1]; ++p) {
+        double4 d = nd[p];
+        if (d.w >= rc) continue;
+        int zb = Z[nj[p]];
+        bool zi1 = Z1 == 0 || za == Z1, zj2 = Z2 == 0 || zb == Z2, zi2 = Z2 == 0 || za == Z2, zj1 = Z1 == 0 || zb == Z1;
+        if (!((zi1 && zj2) || (zi2 && zj1))) continue;
+        double r = d.w, e = 0, de = 0;
+        for (int s = 0; s < M; ++s) {
+            double t = r - X[s];
+            double k = coef[s] * exp(-0.5 * t * t * it2);
+            e += k;
+            de -= k * t * it2;
+        }
+        double f, df;
+        fcut(r, rc, w, f, df);
+        double g = de * f + e * df;
+        double ir = 1.0 / r;
+        fpair[3 * (size_t)p] += g * d.x * ir;
+        fpair[3 * (size_t)p + 1] += g * d.y * ir;
+        fpair[3 * (size_t)p + 2] += g * d.z * ir;
+        epair[p] += 0.5 * e * f;
+    }
+}
+
+__global__ void k_gather(int n, const int* __restrict__ Z, const int* __restrict__ mask, const int* __restrict__ off,
+                         const int* __restrict__ rev, const double4* __restrict__ nd, const double* __restrict__ fpair,
+                         const double* __restrict__ epair, const double* __restrict__ eatom, const double* __restrict__ e0,
+                         double escale, double* __restrict__ le, double* __restrict__ F, double* __restrict__ LV) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    double f0 = 0, f1 = 0, f2 = 0, e = eatom[a];
+    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int p = off[a]; p < off[a + 1]; ++p) {
+        int q = rev[p];
+        double4 d = nd[p];
+        double g0 = fpair[3 * (size_t)q], g1 = fpair[3 * (size_t)q + 1], g2 = fpair[3 * (size_t)q + 2];
+        f0 += fpair[3 * (size_t)p] - g0;
+        f1 += fpair[3 * (size_t)p + 1] - g1;
+        f2 += fpair[3 * (size_t)p + 2] - g2;
+        // virial_a(r, c) -= (-d)(r) f_rev(c)   (column-major 3x3)
+        double dd[3] = {d.x, d.y, d.z}, gg[3] = {g0, g1, g2};
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) v[3 * cc + r] += dd[r] * gg[cc];
+        e += epair[p] + epair[q];
+    }
+    if (!mask || mask[a]) {
+        int z = Z[a];
+        e += (z >= 0 && z < 128) ? e0[z] : 0.0;
+    }
+    le[a] = escale * e;
+    F[3 * (size_t)a] = escale * f0;
+    F[3 * (size_t)a + 1] = escale * f1;
+    F[3 * (size_t)a + 2] = escale * f2;
+    for (int k = 0; k < 9; ++k) LV[9 * (size_t)a + k] = escale * v[k];
+}
+
+// Deterministic single-block sums: E = sum le, virial = sum LV.
+__global__ void k_reduce(int n, const double* __restrict__ le, const double* __restrict__ LV, double* __restrict__ out) {
+    __shared__ double sh[10][256];
+    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = threadIdx.x; a < n; a += blockDim.x) {
+        acc[0] += le[a];
+        for (int k = 0; k < 9; ++k) acc[1 + k] += LV[9 * (size_t)a + k];
+    }
+    for (int k = 0; k < 10; ++k) sh[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int k = 0; k < 10; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x < 10) out[threadIdx.x] = sh[threadIdx.x][0];
+}
+
+}  // namespace
+
+int pair_2b(gapgpu_context& c, const Coordinate& co, int n, const int* d_mask) {
+    if (co.cov != COV_ARD_SE) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "distance_2b needs the ard_se covariance");
+    const int TB = 128;
+    k_pair_2b<<<(n + TB - 1) / TB, TB, 0, c.stream>>>(n, c.Z.as<int>(), d_mask, c.nbr_off.as<int>(), c.nbr_j.as<int>(),
+                                                     c.nbr_d.as<double4>(), co.d2_rc, co.d2_w, co.d2_Z1, co.d2_Z2, co.M,
+                                                     co.dX64, co.dcoef, co.theta[0], c.fpair.as<double>(),
+                                                     c.epair.as<double>());
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
+int gather_outputs(gapgpu_context& c, const gapgpu_model& m, int n, const int* d_mask) {
+    int rc;
+    if ((rc = c.out_le.ensure(sizeof(double) * n)) || (rc = c.out_f.ensure(sizeof(double) * 3 * n)) ||
+        (rc = c.out_lv.ensure(sizeof(double) * 9 * n)) || (rc = c.out_e.ensure(sizeof(double) * (10 + 128))))
+        return rc;
+    double* e0 = c.out_e.as<double>() + 10;
+    GG_CUDA(cudaMemcpyAsync(e0, m.e0, sizeof(double) * 128, cudaMemcpyHostToDevice, c.stream));
+    const int TB = 128;
+    k_gather<<<(n + TB - 1) / TB, TB, 0, c.stream>>>(n, c.Z.as<int>(), d_mask, c.nbr_off.as<int>(), c.nbr_rev.as<int>(),
+                                                    c.nbr_d.as<double4>(), c.fpair.as<double>(), c.epair.as<double>(),
+                                                    c.eatom.as<double>(), e0, m.E_scale, c.out_le.as<double>(),
+                                                    c.out_f.as<double>(), c.out_lv.as<double>());
+    k_reduce<<<1, 256, 0, c.stream>>>(n, c.out_le.as<double>(), c.out_lv.as<double>(), c.out_e.as<double>());
+    c.launches += 2;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
+}  // namespace gapgpu

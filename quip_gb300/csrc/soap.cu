@@ -1,0 +1,542 @@
+// soap.cu -- K3/K4 SOAP expansion, power spectrum and normalisation (forward) and
+// K4^T/K7 adjoint: dE/dq -> dE/dp -> dE/dc -> per-pair force contributions.
+//
+// The descriptor is GAP's `soap` (descriptors_module of the libAtoms/GAP submodule,
+// absent from the reference checkout).  Its conventions were recovered from the
+// reference's fixtures (tests/Si.soap.cur_points.json, tests/test_descriptor.py):
+//   rho_j(r_b) collocation : exp(-alpha (r^2 + r_b^2)) i_l(2 alpha r r_b), written with
+//                            exp(-alpha (r -+ r_b)^2) and the upward recurrence
+//                            i_l = i_{l-2} - (2l-1)/x i_{l-1}
+//   radial coefficients     : R_nl(r) = fc(r) sum_a rho_l(r, r_a) T_an
+//   expansion               : c[s][n][lm] = sum_{j in species s, r_ij < rc} R_nl(r_ij) Y_lm(r^_ij)
+//                            + central atom (l = 0, own species channel)
+//   power spectrum          : p[(ia,jb<=ia), l] = sqrt2^(ia!=jb) / sqrt(2l+1) sum_m c_ia,lm c_jb,lm
+//   descriptor              : q = p / |p|, q[dim-1] = covariance_sigma0
+// Real orthonormal spherical harmonics replace GAP's complex ones; the power
+// spectrum is invariant under that unitary change of basis.
+//
+// Gradients are never materialised as dq/dr (3*dim per pair).  The backward pass
+// contracts dE/dq with the normalisation Jacobian (FP64), forms
+// dE/dc[a][lm] = sum_b H_l[a][b] c[b][lm], and for each pair computes
+// f_ij = dE_i/dr_j = sum_{n,lm} dE/dc[s_j][n][lm] d(R_nl Y_lm)/dr_j, which is exactly
+// the reference's matmul(gradPredict, grad_data(:,:,n)) (IPModel_GAP.f95:479) for the
+// neighbour entry n = j; the centre entry is minus the sum over neighbours.
+#include <cub/cub.cuh>
+#include <cmath>
+#include "context.h"
+
+namespace gapgpu {
+
+__constant__ double c_ylm_norm[(MAX_LMAX + 1) * (MAX_LMAX + 1)];  // N_lm (sqrt2 folded in for m>0)
+
+namespace {
+
+template <class R>
+struct Dual {  // value and gradient with respect to the neighbour's displacement
+    R v, x, y, z;
+};
+template <class R> __device__ __forceinline__ Dual<R> dmul(const Dual<R>& a, const Dual<R>& b) {
+    return {a.v * b.v, a.x * b.v + a.v * b.x, a.y * b.v + a.v * b.y, a.z * b.v + a.v * b.z};
+}
+template <class R> __device__ __forceinline__ Dual<R> dsub(const Dual<R>& a, const Dual<R>& b) {
+    return {a.v - b.v, a.x - b.x, a.y - b.y, a.z - b.z};
+}
+template <class R> __device__ __forceinline__ Dual<R> dadd(const Dual<R>& a, const Dual<R>& b) {
+    return {a.v + b.v, a.x + b.x, a.y + b.y, a.z + b.z};
+}
+template <class R> __device__ __forceinline__ Dual<R> dscale(R s, const Dual<R>& a) { return {s * a.v, s * a.x, s * a.y, s * a.z}; }
+
+__device__ __forceinline__ double rexp(double x) { return exp(x); }
+__device__ __forceinline__ float rexp(float x) { return __expf(x); }
+__device__ __forceinline__ double rcos(double x) { return cos(x); }
+__device__ __forceinline__ float rcos(float x) { return cosf(x); }
+__device__ __forceinline__ double rsin(double x) { return sin(x); }
+__device__ __forceinline__ float rsin(float x) { return sinf(x); }
+
+// coordination_function and its derivative
+template <class R>
+__device__ __forceinline__ void cutoff_fn(R r, R rc, R w, R& f, R& df) {
+    if (r > rc) { f = 0; df = 0; return; }
+    if (r > rc - w) {
+        const R pi = (R)3.14159265358979323846;
+        R a = pi * (r - rc + w) / w;
+        f = (R)0.5 * (rcos(a) + (R)1);
+        df = -(R)0.5 * pi * rsin(a) / w;
+        return;
+    }
+    f = 1; df = 0;
+}
+
+// Column m of the real spherical harmonics Y_lm(d/|d|), l = m..l_max, written to
+// Y[l*l + l +- m].  t = z/r; (cm + i sm) = ((x + i y)/r)^m.
+template <class R>
+__device__ void ylm_column(int m, int L, R xr, R yr, R t, R* Y) {
+    R cm = 1, sm = 0;
+    for (int k = 0; k < m; ++k) {
+        R c2 = cm * xr - sm * yr;
+        sm = sm * xr + cm * yr;
+        cm = c2;
+    }
+    R qmm = 1;
+    for (int k = 1; k <= 2 * m - 1; k += 2) qmm *= (R)k;
+    R q2 = qmm, q1 = 0;
+    for (int l = m; l < L; ++l) {
+        R q;
+        if (l == m) q = qmm;
+        else if (l == m + 1) q = (R)(2 * m + 1) * t * qmm;
+        else q = ((R)(2 * l - 1) * t * q1 - (R)(l + m - 1) * q2) / (R)(l - m);
+        if (l > m) q2 = q1;
+        q1 = q;
+        if (l == m) q2 = 0;
+        R nrm = (R)c_ylm_norm[l * l + m];
+        if (m == 0) Y[l * l + l] = nrm * q;
+        else {
+            Y[l * l + l + m] = nrm * q * cm;
+            Y[l * l + l - m] = nrm * q * sm;
+        }
+    }
+}
+
+// Same column with gradients (dual arithmetic on x, y, z).
+template <class R>
+__device__ void ylm_column_grad(int m, int L, R dx, R dy, R dz, R r, Dual<R>* Y) {
+    R ir = (R)1 / r;
+    // xr = x/r etc. with d(x/r)/dx_k = (delta_xk - x x_k / r^2)/r
+    R xr = dx * ir, yr = dy * ir, zr = dz * ir;
+    Dual<R> X = {xr, (1 - xr * xr) * ir, -xr * yr * ir, -xr * zr * ir};
+    Dual<R> Yv = {yr, -yr * xr * ir, (1 - yr * yr) * ir, -yr * zr * ir};
+    Dual<R> T = {zr, -zr * xr * ir, -zr * yr * ir, (1 - zr * zr) * ir};
+    Dual<R> cm = {1, 0, 0, 0}, sm = {0, 0, 0, 0};
+    for (int k = 0; k < m; ++k) {
+        Dual<R> c2 = dsub(dmul(cm, X), dmul(sm, Yv));
+        sm = dadd(dmul(sm, X), dmul(cm, Yv));
+        cm = c2;
+    }
+    R qmm = 1;
+    for (int k = 1; k <= 2 * m - 1; k += 2) qmm *= (R)k;
+    Dual<R> q1 = {0, 0, 0, 0}, q2 = {0, 0, 0, 0};
+    for (int l = m; l < L; ++l) {
+        Dual<R> q;
+        if (l == m) q = {qmm, 0, 0, 0};
+        else if (l == m + 1) q = dscale((R)(2 * m + 1) * qmm, T);
+        else q = dscale((R)1 / (R)(l - m), dsub(dscale((R)(2 * l - 1), dmul(T, q1)), dscale((R)(l + m - 1), q2)));
+        q2 = (l == m) ? Dual<R>{0, 0, 0, 0} : q1;
+        q1 = q;
+        R nrm = (R)c_ylm_norm[l * l + m];
+        if (m == 0) Y[l * l + l] = dscale(nrm, q);
+        else {
+            Y[l * l + l + m] = dscale(nrm, dmul(q, cm));
+            Y[l * l + l - m] = dscale(nrm, dmul(q, sm));
+        }
+    }
+}
+
+// rho_l(r, r_b) for l = 0..L-1 and (optionally) d/dr.
+template <class R>
+__device__ void radial_collocation(R r, R rb, R alpha, int L, R* out, R* dout) {
+    if (rb == (R)0) {
+        R e = rexp(-alpha * r * r);
+        out[0] = e;
+        if (dout) dout[0] = -(R)2 * alpha * r * e;
+        for (int l = 1; l < L; ++l) { out[l] = 0; if (dout) dout[l] = 0; }
+        return;
+    }
+    R x = (R)2 * alpha * r * rb;
+    R em = rexp(-alpha * (r - rb) * (r - rb));
+    R ep = rexp(-alpha * (r + rb) * (r + rb));
+    R ix = (R)1 / x;
+    out[0] = (R)0.5 * (em - ep) * ix;
+    if (L > 1) out[1] = (R)0.5 * (em + ep) * ix - (R)0.5 * (em - ep) * ix * ix;
+    for (int l = 2; l < L; ++l) out[l] = out[l - 2] - (R)(2 * l - 1) * out[l - 1] * ix;
+    if (dout) {
+        // d/dr with dx/dr = 2 alpha rb, dem/dr = -2 alpha (r - rb) em, dep/dr = -2 alpha (r + rb) ep
+        R dx = (R)2 * alpha * rb;
+        R dem = -(R)2 * alpha * (r - rb) * em, dep = -(R)2 * alpha * (r + rb) * ep;
+        R dix = -dx * ix * ix;
+        dout[0] = (R)0.5 * (dem - dep) * ix + (R)0.5 * (em - ep) * dix;
+        if (L > 1)
+            dout[1] = (R)0.5 * (dem + dep) * ix + (R)0.5 * (em + ep) * dix - (R)0.5 * (dem - dep) * ix * ix -
+                      (R)0.5 * (em - ep) * (R)2 * ix * dix;
+        for (int l = 2; l < L; ++l) dout[l] = dout[l - 2] - (R)(2 * l - 1) * (dout[l - 1] * ix + out[l - 1] * dix);
+    }
+}
+
+__device__ __forceinline__ int species_channel(const SoapConst& sc, int z) {
+    for (int s = 0; s < sc.n_species; ++s)
+        if (sc.species_Z[s] == z || sc.species_Z[s] == 0) return s;
+    return -1;
+}
+
+__device__ __forceinline__ void decode_pair(int pr, int& ia, int& jb) {
+    int a = (int)((sqrt(8.0 * pr + 1.0) - 1.0) * 0.5);
+    while ((a + 1) * (a + 2) / 2 <= pr) ++a;
+    while (a * (a + 1) / 2 > pr) --a;
+    ia = a;
+    jb = pr - a * (a + 1) / 2;
+}
+
+constexpr int FWD_THREADS = 128;
+constexpr int NBC = 16;  // neighbours staged per chunk
+
+// Forward: one block per centre.
+template <class R>
+__global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int nc, const int* __restrict__ centres,
+                                                               const int* __restrict__ Z, const int* __restrict__ off,
+                                                               const int* __restrict__ nj, const double4* __restrict__ nd,
+                                                               R* __restrict__ c_out, R* __restrict__ q_out,
+                                                               double* __restrict__ pnorm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ci = blockIdx.x;
+    if (ci >= nc) return;
+    const int atom = centres[ci];
+    const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, nmL = nm * L;
+    R* cs = reinterpret_cast<R*>(smem_raw);        // ncomp
+    R* Ysm = cs + sc.ncomp;                        // NBC * L2
+    R* tmp = Ysm + NBC * L2;                       // NBC * nm * L   (collocation)
+    R* Rsm = tmp + NBC * nmL;                      // NBC * nm * L   (radial coefficients)
+    R* fcs = Rsm + NBC * nmL;                      // NBC
+    int* spc = reinterpret_cast<int*>(fcs + NBC);  // NBC
+    const int tid = threadIdx.x;
+    for (int k = tid; k < sc.ncomp; k += blockDim.x) cs[k] = 0;
+    const int p0 = off[atom], p1 = off[atom + 1];
+    for (int base = p0; base < p1; base += NBC) {
+        const int cnt = min(NBC, p1 - base);
+        __syncthreads();
+        // per neighbour: species channel, cutoff function
+        if (tid < cnt) {
+            double4 d = nd[base + tid];
+            int s = (d.w < sc.rc) ? species_channel(sc, Z[nj[base + tid]]) : -1;
+            spc[tid] = s;
+            R f, df;
+            cutoff_fn<R>((R)d.w, (R)sc.rc, (R)sc.w, f, df);
+            fcs[tid] = f;
+        }
+        __syncthreads();
+        // Y_lm columns: (t, m)
+        for (int k = tid; k < cnt * L; k += blockDim.x) {
+            int t = k / L, m = k % L;
+            if (spc[t] < 0) continue;
+            double4 d = nd[base + t];
+            R ir = (R)1 / (R)d.w;
+            ylm_column<R>(m, L, (R)d.x * ir, (R)d.y * ir, (R)d.z * ir, Ysm + t * L2);
+        }
+        // collocation: (t, a)
+        for (int k = tid; k < cnt * nm; k += blockDim.x) {
+            int t = k / nm, a = k % nm;
+            if (spc[t] < 0) continue;
+            radial_collocation<R>((R)nd[base + t].w, (R)sc.rb[a], (R)sc.alpha, L, tmp + t * nmL + a * L, nullptr);
+        }
+        __syncthreads();
+        // R_nl = fc sum_a T_an rho_al : (t, n, l)
+        for (int k = tid; k < cnt * nmL; k += blockDim.x) {
+            int t = k / nmL, r = k % nmL, n = r / L, l = r % L;
+            if (spc[t] < 0) continue;
+            R acc = 0;
+            for (int a = 0; a < nm; ++a) acc += (R)sc.T[a * nm + n] * tmp[t * nmL + a * L + l];
+            Rsm[t * nmL + n * L + l] = acc * fcs[t];
+        }
+        __syncthreads();
+        // accumulate c[s][n][lm]
+        for (int k = tid; k < sc.ncomp; k += blockDim.x) {
+            int s = k / (nm * L2), r = k % (nm * L2), n = r / L2, lm = r % L2;
+            int l = (int)sqrtf((float)lm);
+            if ((l + 1) * (l + 1) <= lm) ++l;
+            R acc = 0;
+            for (int t = 0; t < cnt; ++t)
+                if (spc[t] == s) acc += Rsm[t * nmL + n * L + l] * Ysm[t * L2 + lm];
+            cs[k] += acc;
+        }
+    }
+    __syncthreads();
+    // central atom
+    const int zc = Z[atom];
+    for (int k = tid; k < sc.n_species * nm; k += blockDim.x) {
+        int s = k / nm, n = k % nm;
+        if (sc.centre_all || sc.species_Z[s] == zc || sc.species_Z[s] == 0) cs[(s * nm + n) * L2] += (R)sc.centre_R[n];
+    }
+    __syncthreads();
+    R* cg = c_out + (size_t)ci * sc.ncomp;
+    for (int k = tid; k < sc.ncomp; k += blockDim.x) cg[k] = cs[k];
+    // power spectrum (reuse staging area)
+    R* ps = Ysm;
+    const int np = sc.n_pairs * L;
+    double ss = 0;
+    for (int k = tid; k < np; k += blockDim.x) {
+        int pr = k / L, l = k % L, ia, jb;
+        decode_pair(pr, ia, jb);
+        R v = 0;
+        const R* ca = cs + ia * L2 + l * l;
+        const R* cb = cs + jb * L2 + l * l;
+        for (int m = 0; m < 2 * l + 1; ++m) v += ca[m] * cb[m];
+        R fac = (ia != jb ? (R)1.41421356237309504880 : (R)1) * rsqrt((R)(2 * l + 1));
+        v *= fac;
+        ps[k] = v;
+        ss += (double)v * (double)v;
+    }
+    // block reduction of |p|^2 in FP64
+    typedef cub::BlockReduce<double, FWD_THREADS> BR;
+    __shared__ typename BR::TempStorage tmps;
+    double tot = BR(tmps).Sum(ss);
+    __shared__ double s_norm;
+    if (tid == 0) {
+        s_norm = sqrt(tot);
+        pnorm[ci] = s_norm;
+    }
+    __syncthreads();
+    const double inv = sc.normalise ? 1.0 / s_norm : 1.0;
+    R* qg = q_out + (size_t)ci * sc.dpad;
+    for (int k = tid; k < sc.dpad; k += blockDim.x) {
+        R v;
+        if (k < np) v = (R)((double)ps[k] * inv);
+        else if (k == np) v = (R)sc.sigma0;
+        else v = 0;
+        qg[k] = v;
+    }
+}
+
+constexpr int BWD_THREADS = 128;
+constexpr int BWD_WARPS = BWD_THREADS / 32;
+
+// Backward: one block per centre; warps take neighbours.
+template <class R>
+__global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, int nc, const int* __restrict__ centres,
+                                                                const int* __restrict__ Z, const int* __restrict__ off,
+                                                                const int* __restrict__ nj, const double4* __restrict__ nd,
+                                                                const R* __restrict__ c_in, const R* __restrict__ q_in,
+                                                                const double* __restrict__ pnorm, const R* __restrict__ G,
+                                                                double* __restrict__ fpair) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ci = blockIdx.x;
+    if (ci >= nc) return;
+    const int atom = centres[ci];
+    const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, nmL = nm * L, NN = sc.n_species * nm;
+    const int np = sc.n_pairs * L;
+    R* cs = reinterpret_cast<R*>(smem_raw);  // ncomp
+    R* dc = cs + sc.ncomp;                   // ncomp (dE/dc)
+    R* dp = dc + sc.ncomp;                   // np    (dE/dp)
+    R* wbase = dp + np;                      // per warp: Y dual (4 L2) + rho (2 nmL) + R (2 nmL)
+    const int per_warp = 4 * L2 + 4 * nmL;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const R* cg = c_in + (size_t)ci * sc.ncomp;
+    for (int k = tid; k < sc.ncomp; k += blockDim.x) cs[k] = cg[k];
+    // dE/dp = (G - q (q.G)) / |p|   (FP64)
+    const R* qg = q_in + (size_t)ci * sc.dpad;
+    const R* gg = G + (size_t)ci * sc.dpad;
+    double qd = 0;
+    for (int k = tid; k < np; k += blockDim.x) qd += (double)qg[k] * (double)gg[k];
+    typedef cub::BlockReduce<double, BWD_THREADS> BR;
+    __shared__ typename BR::TempStorage tmps;
+    double tot = BR(tmps).Sum(qd);
+    __shared__ double s_qg;
+    if (tid == 0) s_qg = tot;
+    __syncthreads();
+    const double nrm = pnorm[ci];
+    for (int k = tid; k < np; k += blockDim.x) {
+        double v = sc.normalise ? ((double)gg[k] - (double)qg[k] * s_qg) / nrm : (double)gg[k];
+        int l = k % L;
+        int pr = k / L, ia, jb;
+        decode_pair(pr, ia, jb);
+        double fac = (ia != jb ? 1.41421356237309504880 : 2.0) / sqrt((double)(2 * l + 1));
+        dp[k] = (R)(v * fac);  // H_l[ia][jb] (= H_l[jb][ia])
+    }
+    __syncthreads();
+    // dE/dc[a][lm] = sum_b H_l[a][b] c[b][lm]
+    for (int k = tid; k < sc.ncomp; k += blockDim.x) {
+        int a = k / L2, lm = k % L2;
+        int l = (int)sqrtf((float)lm);
+        if ((l + 1) * (l + 1) <= lm) ++l;
+        R acc = 0;
+        for (int b = 0; b < NN; ++b) {
+            int hi = a > b ? a : b, lo = a > b ? b : a;
+            acc += dp[(hi * (hi + 1) / 2 + lo) * L + l] * cs[b * L2 + lm];
+        }
+        dc[k] = acc;
+    }
+    __syncthreads();
+    // per-pair contraction
+    R* wY = wbase + wid * per_warp;            // 4*L2  (v, x, y, z interleaved as Dual)
+    R* wrho = wY + 4 * L2;                     // 2*nmL (rho, drho)
+    R* wR = wrho + 2 * nmL;                    // 2*nmL (R, dR)
+    Dual<R>* Yd = reinterpret_cast<Dual<R>*>(wY);
+    const int p0 = off[atom], p1 = off[atom + 1];
+    for (int p = p0 + wid; p < p1; p += BWD_WARPS) {
+        double4 d = nd[p];
+        int s = (d.w < sc.rc) ? species_channel(sc, Z[nj[p]]) : -1;
+        if (s < 0) continue;  // warp-uniform
+        R r = (R)d.w, ir = (R)1 / r;
+        for (int m = lane; m < L; m += 32) ylm_column_grad<R>(m, L, (R)d.x, (R)d.y, (R)d.z, r, Yd);
+        for (int a = lane; a < nm; a += 32)
+            radial_collocation<R>(r, (R)sc.rb[a], (R)sc.alpha, L, wrho + a * L, wrho + nmL + a * L);
+        __syncwarp();
+        R f, df;
+        cutoff_fn<R>(r, (R)sc.rc, (R)sc.w, f, df);
+        for (int k = lane; k < nmL; k += 32) {
+            int n = k / L, l = k % L;
+            R a0 = 0, a1 = 0;
+            for (int a = 0; a < nm; ++a) {
+                R t = (R)sc.T[a * nm + n];
+                a0 += t * wrho[a * L + l];
+                a1 += t * wrho[nmL + a * L + l];
+            }
+            wR[k] = a0 * f;
+            wR[nmL + k] = a1 * f + a0 * df;
+        }
+        __syncwarp();
+        R fx = 0, fy = 0, fz = 0;
+        const R ux = (R)d.x * ir, uy = (R)d.y * ir, uz = (R)d.z * ir;
+        const R* dcs = dc + s * nm * L2;
+        for (int k = lane; k < nm * L2; k += 32) {
+            int n = k / L2, lm = k % L2;
+            int l = (int)sqrtf((float)lm);
+            if ((l + 1) * (l + 1) <= lm) ++l;
+            R g = dcs[k];
+            R Rv = wR[n * L + l], dR = wR[nmL + n * L + l];
+            Dual<R> y = Yd[lm];
+            R rad = g * dR * y.v;
+            fx += rad * ux + g * Rv * y.x;
+            fy += rad * uy + g * Rv * y.y;
+            fz += rad * uz + g * Rv * y.z;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, o);
+            fy += __shfl_xor_sync(0xffffffffu, fy, o);
+            fz += __shfl_xor_sync(0xffffffffu, fz, o);
+        }
+        if (lane == 0) {
+            fpair[3 * (size_t)p] += (double)fx;
+            fpair[3 * (size_t)p + 1] += (double)fy;
+            fpair[3 * (size_t)p + 2] += (double)fz;
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void k_centre_flags(int n, const int* __restrict__ Z, const int* __restrict__ mask, SoapConst sc, int nZ,
+                               const int* __restrict__ zlist, int* __restrict__ flags) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    int ok = 0;
+    for (int k = 0; k < nZ; ++k) if (zlist[k] == Z[a] || zlist[k] == 0) ok = 1;
+    if (mask && !mask[a]) ok = 0;
+    flags[a] = ok;
+}
+
+__global__ void k_iota(int n, int* out) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < n) out[a] = a;
+}
+
+bool g_norm_ready[64] = {false};
+
+int ensure_ylm_norm() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && g_norm_ready[dev]) return GAPGPU_OK;
+    double h[(MAX_LMAX + 1) * (MAX_LMAX + 1)] = {0};
+    for (int l = 0; l <= MAX_LMAX; ++l)
+        for (int m = 0; m <= l; ++m) {
+            double lf = 1.0;
+            for (int k = l - m + 1; k <= l + m; ++k) lf /= k;
+            double N = std::sqrt((2 * l + 1) / (4.0 * M_PI) * lf);
+            h[l * l + m] = m == 0 ? N : std::sqrt(2.0) * N;
+        }
+    GG_CUDA(cudaMemcpyToSymbol(c_ylm_norm, h, sizeof h));
+    if (dev < 64) g_norm_ready[dev] = true;
+    return GAPGPU_OK;
+}
+
+template <class R>
+size_t fwd_smem(const SoapConst& sc) {
+    const int L = sc.l_max + 1, L2 = L * L, nmL = sc.n_max * L;
+    size_t ps = (size_t)sc.n_pairs * L;
+    size_t stage = (size_t)NBC * L2 + 2 * (size_t)NBC * nmL + NBC;
+    return sizeof(R) * ((size_t)sc.ncomp + std::max(stage, ps)) + sizeof(int) * NBC + 16;
+}
+template <class R>
+size_t bwd_smem(const SoapConst& sc) {
+    const int L = sc.l_max + 1, L2 = L * L, nmL = sc.n_max * L;
+    return sizeof(R) * (2 * (size_t)sc.ncomp + (size_t)sc.n_pairs * L + BWD_WARPS * (4 * (size_t)L2 + 4 * (size_t)nmL)) + 16;
+}
+
+template <class R>
+int launch_forward(gapgpu_context& c, const Coordinate& co, int nc) {
+    SoapConst sc = soap_const(co);
+    size_t sm = fwd_smem<R>(sc);
+    if (sm > 200 * 1024) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the shared-memory forward kernel");
+    GG_CUDA(cudaFuncSetAttribute(k_soap_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_soap_forward<R><<<nc, FWD_THREADS, sm, c.stream>>>(sc, nc, c.centres.as<int>(), c.Z.as<int>(), c.nbr_off.as<int>(),
+                                                         c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.scratch.as<R>(),
+                                                         c.qbuf.as<R>(), c.pnorm.as<double>());
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
+template <class R>
+int launch_backward(gapgpu_context& c, const Coordinate& co, int nc) {
+    SoapConst sc = soap_const(co);
+    size_t sm = bwd_smem<R>(sc);
+    if (sm > 200 * 1024) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the shared-memory backward kernel");
+    GG_CUDA(cudaFuncSetAttribute(k_soap_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_soap_backward<R><<<nc, BWD_THREADS, sm, c.stream>>>(sc, nc, c.centres.as<int>(), c.Z.as<int>(), c.nbr_off.as<int>(),
+                                                          c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.scratch.as<R>(),
+                                                          c.qbuf.as<R>(), c.pnorm.as<double>(), c.Gbuf.as<R>(),
+                                                          c.fpair.as<double>());
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
+}  // namespace
+
+int select_centres(gapgpu_context& c, const Coordinate& co, int n, const int* d_mask, int* nc_out) {
+    int rc;
+    if ((rc = c.flags.ensure(sizeof(int) * n)) || (rc = c.centres.ensure(sizeof(int) * n)) ||
+        (rc = c.ncent.ensure(sizeof(int) * 2)) || (rc = c.eatom.ensure(sizeof(double) * n)))
+        return rc;
+    if ((rc = ensure_ylm_norm())) return rc;
+    SoapConst sc = soap_const(co);
+    int zl[MAX_CENTRE_Z];
+    for (int k = 0; k < co.soap.n_Z; ++k) zl[k] = co.soap.Z[k];
+    int* dz = c.ncent.as<int>();
+    (void)dz;
+    // small Z list through a kernel argument copy
+    if ((rc = c.minmax.ensure(sizeof(int) * MAX_CENTRE_Z + 64))) return rc;
+    GG_CUDA(cudaMemcpyAsync(c.minmax.p, zl, sizeof(int) * co.soap.n_Z, cudaMemcpyHostToDevice, c.stream));
+    const int TB = 256, nb = (n + TB - 1) / TB;
+    k_centre_flags<<<nb, TB, 0, c.stream>>>(n, c.Z.as<int>(), d_mask, sc, co.soap.n_Z, c.minmax.as<int>(), c.flags.as<int>());
+    k_iota<<<nb, TB, 0, c.stream>>>(n, c.atom_idx.as<int>());
+    c.launches += 2;
+    size_t tmp = 0;
+    cub::DeviceSelect::Flagged(nullptr, tmp, c.atom_idx.as<int>(), c.flags.as<int>(), c.centres.as<int>(), c.ncent.as<int>(),
+                               n, c.stream);
+    if ((rc = c.cub_tmp.ensure(tmp))) return rc;
+    GG_CUDA(cub::DeviceSelect::Flagged(c.cub_tmp.p, tmp, c.atom_idx.as<int>(), c.flags.as<int>(), c.centres.as<int>(),
+                                       c.ncent.as<int>(), n, c.stream));
+    int nc = 0;
+    GG_CUDA(cudaMemcpyAsync(&nc, c.ncent.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    GG_CUDA(cudaStreamSynchronize(c.stream));
+    *nc_out = nc;
+    return GAPGPU_OK;
+}
+
+int soap_forward(gapgpu_context& c, const Coordinate& co, int n, int nc) {
+    (void)n;
+    SoapConst sc = soap_const(co);
+    const bool mixed = c.precision != GAPGPU_FP64;
+    const size_t rs = mixed ? sizeof(float) : sizeof(double);
+    int rc;
+    if ((rc = c.scratch.ensure(rs * (size_t)nc * sc.ncomp)) || (rc = c.qbuf.ensure(rs * (size_t)nc * sc.dpad)) ||
+        (rc = c.pnorm.ensure(sizeof(double) * nc)))
+        return rc;
+    if (nc == 0) return GAPGPU_OK;
+    return mixed ? launch_forward<float>(c, co, nc) : launch_forward<double>(c, co, nc);
+}
+
+int soap_backward(gapgpu_context& c, const Coordinate& co, int n, int nc) {
+    (void)n;
+    if (nc == 0) return GAPGPU_OK;
+    return c.precision != GAPGPU_FP64 ? launch_backward<float>(c, co, nc) : launch_backward<double>(c, co, nc);
+}
+
+}  // namespace gapgpu

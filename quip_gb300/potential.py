@@ -1,0 +1,181 @@
+"""Potential: the host-side mirror of QUIP's Potential API for the GAP path.
+
+Mirrors quippy's ``Potential`` (quippy/quippy/potential.py:64-108 init, :177-325
+calculate) and the Fortran ``potential_Filename_Initialise`` /
+``potential_calc(pot, at, energy=, force=, virial=, local_energy=, local_virial=,
+args_str=)`` (src/Potentials/Potential.f95:438-468, :803-996) for a GAP parameter file.
+Every number is computed by libgapgpu.so on the GPU; this module only moves arrays.
+"""
+import os
+import re
+
+import numpy as np
+
+from . import _lib
+from .atoms import Atoms
+
+
+def _init_args_from_xml(xml):
+    """Default init args from the first <Potential init_args=...> tag (Potential.f95:525-538)."""
+    m = re.search(r'<Potential[^>]*init_args="([^"]*)"', xml)
+    return m.group(1) if m else "IP GAP"
+
+
+class Potential:
+    """GAP potential evaluated on a GB300.
+
+    Potential(args_str="IP GAP label=...", param_filename="gap.xml", precision="fp64")
+
+    ``precision`` is "fp64" (plain path, matches the reference within 1e-8 eV/atom
+    and 1e-7 eV/A), "bf16x3" or "tf32" (mixed path: FP32 SOAP, tensor-core kernel GEMMs).
+    """
+
+    def __init__(self, args_str="", param_filename=None, param_str=None, precision="fp64"):
+        if (param_filename is None) == (param_str is None):
+            raise ValueError("give exactly one of param_filename / param_str")
+        if param_filename is not None:
+            with open(param_filename) as f:
+                xml = f.read()
+            base = os.path.dirname(os.path.abspath(param_filename))
+        else:
+            xml, base = param_str, os.getcwd()
+        if not args_str.strip():
+            args_str = _init_args_from_xml(xml)
+        toks = args_str.split()
+        if "GAP" not in toks:
+            raise ValueError("only 'IP GAP' potentials are handled by this library: %r" % args_str)
+        self.args_str = args_str
+        self.param_filename = param_filename
+        self.precision = precision
+        L = _lib.load()
+        self._L = L
+        h = _lib.ctypes.c_void_p()
+        xb = xml.encode()
+        _lib.check(L.gapgpu_model_create(xb, len(xb), args_str.encode(), base.encode(), _lib.ctypes.byref(h)))
+        self._model = h
+        c = _lib.ctypes.c_void_p()
+        _lib.check(L.gapgpu_context_create(self._model, _lib.PRECISIONS[precision], _lib.ctypes.byref(c)))
+        self._ctx = c
+        self.results = {}
+
+    def __del__(self):
+        L = getattr(self, "_L", None)
+        if L is None:
+            return
+        if getattr(self, "_ctx", None):
+            L.gapgpu_context_destroy(self._ctx)
+            self._ctx = None
+        if getattr(self, "_model", None):
+            L.gapgpu_model_destroy(self._model)
+            self._model = None
+
+    # ------------------------------------------------------------------ info
+    def cutoff(self):
+        v = _lib.ctypes.c_double()
+        _lib.check(self._L.gapgpu_model_cutoff(self._model, _lib.ctypes.byref(v)))
+        return v.value
+
+    def info(self):
+        n = _lib.ctypes.c_int()
+        dims = (_lib.ctypes.c_int * 64)()
+        ns = (_lib.ctypes.c_int * 64)()
+        _lib.check(self._L.gapgpu_model_info(self._model, _lib.ctypes.byref(n), dims, ns, 64))
+        return [(dims[k], ns[k]) for k in range(n.value)]
+
+    def timings(self):
+        ms = (_lib.ctypes.c_double * 7)()
+        k = self._L.gapgpu_context_timings(self._ctx, ms, 7)
+        names = ["neighbours", "soap_fwd", "gemm", "soap_bwd", "pair2b", "reduce", "total"]
+        return dict(zip(names[:k], list(ms)[:k]))
+
+    def launches(self):
+        v = _lib.ctypes.c_int64()
+        _lib.check(self._L.gapgpu_context_launches(self._ctx, _lib.ctypes.byref(v)))
+        return v.value
+
+    # ------------------------------------------------------------------ calc
+    @staticmethod
+    def _arrays(at):
+        pos = np.ascontiguousarray(at.positions, dtype=np.float64)
+        Z = np.ascontiguousarray(at.numbers, dtype=np.int32)
+        lat = np.asfortranarray(at.lattice, dtype=np.float64).ravel(order="F").copy()
+        pbc = np.ascontiguousarray(np.asarray(at.pbc, dtype=np.int32).reshape(3))
+        return pos, Z, lat, pbc
+
+    def calc(self, at, energy=True, force=True, virial=True, local_energy=False, local_virial=False, args_str="",
+             atom_mask=None):
+        """potential_calc: returns a dict with the requested quantities.
+
+        energy (float), force (N,3), virial (3,3), local_energy (N,), local_virial (N,3,3).
+        ``atom_mask`` is the logical property that args_str atom_mask_name names."""
+        pos, Z, lat, pbc = self._arrays(at)
+        n = len(pos)
+        E = np.zeros(1)
+        F = np.zeros((n, 3)) if force else None
+        V = np.zeros(9) if virial else None
+        LE = np.zeros(n) if local_energy else None
+        LV = np.zeros((n, 9)) if local_virial else None
+        mask = None if atom_mask is None else np.ascontiguousarray(atom_mask, dtype=np.int32)
+        _lib.check(self._L.gapgpu_calc(self._ctx, n, _lib.ptr(pos), _lib.ptr(Z), _lib.ptr(lat), _lib.ptr(pbc),
+                                       _lib.ptr(mask), _lib.ptr(E) if energy else None, _lib.ptr(LE), _lib.ptr(F),
+                                       _lib.ptr(V), _lib.ptr(LV), args_str.encode()))
+        out = {}
+        if energy:
+            out["energy"] = float(E[0])
+        if force:
+            out["force"] = F
+        if virial:
+            out["virial"] = V.reshape(3, 3, order="F")
+        if local_energy:
+            out["local_energy"] = LE
+        if local_virial:
+            out["local_virial"] = LV.reshape(n, 3, 3).transpose(0, 2, 1)
+        self.results = out
+        return out
+
+    def calculate(self, atoms, properties=("energy", "forces", "stress")):
+        """ASE-calculator view (quippy/quippy/potential.py:177-325): forces (N,3),
+        stress = -virial / volume (potential.py:281-284), energies (local)."""
+        r = self.calc(atoms, energy=True, force=True, virial=True, local_energy="energies" in properties)
+        res = {"energy": r["energy"], "free_energy": r["energy"], "forces": r["force"]}
+        res["stress"] = -r["virial"] / atoms.volume()
+        if "energies" in properties:
+            res["energies"] = r["local_energy"]
+        self.results = res
+        return res
+
+    def get_potential_energy(self, atoms):
+        return self.calc(atoms, force=False, virial=False)["energy"]
+
+    def get_forces(self, atoms):
+        return self.calc(atoms, energy=False, virial=False)["force"]
+
+    # ------------------------------------------------------------------ auxiliaries
+    def neighbours(self, at, cutoff=None):
+        """QUIP-semantics neighbour list built on the GPU: (offsets, j, shift)."""
+        pos, Z, lat, pbc = self._arrays(at)
+        n = len(pos)
+        rc = self.cutoff() if cutoff is None else cutoff
+        off = np.zeros(n + 1, np.int32)
+        tot = _lib.ctypes.c_int64()
+        _lib.check(self._L.gapgpu_neighbours(self._ctx, n, _lib.ptr(pos), _lib.ptr(lat), _lib.ptr(pbc), rc,
+                                             _lib.ptr(off), None, None, 0, _lib.ctypes.byref(tot)))
+        j = np.zeros(tot.value, np.int32)
+        sh = np.zeros((tot.value, 3), np.int32)
+        _lib.check(self._L.gapgpu_neighbours(self._ctx, n, _lib.ptr(pos), _lib.ptr(lat), _lib.ptr(pbc), rc,
+                                             _lib.ptr(off), _lib.ptr(j), _lib.ptr(sh), tot.value, _lib.ctypes.byref(tot)))
+        return off, j, sh
+
+    def descriptors(self, at, coordinate=0):
+        """SOAP descriptors of every centre of the given coordinate (n_centres, dim)."""
+        pos, Z, lat, pbc = self._arrays(at)
+        dim = self.info()[coordinate][0]
+        q = np.zeros((len(pos), dim))
+        nc = _lib.ctypes.c_int()
+        _lib.check(self._L.gapgpu_descriptors(self._ctx, coordinate, len(pos), _lib.ptr(pos), _lib.ptr(Z),
+                                              _lib.ptr(lat), _lib.ptr(pbc), _lib.ptr(q), q.size,
+                                              _lib.ctypes.byref(nc)))
+        return q[:nc.value]
+
+
+__all__ = ["Potential", "Atoms"]

@@ -1,0 +1,119 @@
+"""CPU-side checks of the C ABI and the host logic (no GPU compute)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from quip_gb300 import _lib, models
+from oracle import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    hdr = open(os.path.join(ROOT, "include", "gapgpu.h")).read()
+    return sorted(set(re.findall(r"\b(gapgpu_\w+)\s*\(", hdr)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    declared = _declared_symbols()
+    assert declared == sorted(_lib.EXPORTS)
+    for s in declared:
+        assert hasattr(L, s), s
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    for s in declared:
+        assert re.search(r"\bT %s\b" % s, out), s
+
+
+def test_bad_xml_is_rejected_before_device_use():
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    x = b"<GAP><GAP_params label='a'><gpSparse></GAP_params>"
+    rc = L.gapgpu_model_create(x, len(x), b"", b".", ctypes.byref(h))
+    assert rc == _lib.ERR_XML
+    assert b"mismatched" in L.gapgpu_last_error() or b"parse" in L.gapgpu_last_error()
+
+
+def test_unsupported_descriptor_is_rejected(tmp_path):
+    L = _lib.load()
+    p = models.write_gap_xml(str(tmp_path / "g.xml"),
+                             [dict(desc_str="bispectrum_so4 cutoff=3.0 j_max=4", cov="dot_product", delta=1.0, zeta=2.0,
+                                   X=np.ones((2, 5)), alpha=np.ones(2), sc=np.ones(2))])
+    x = open(p, "rb").read()
+    h = ctypes.c_void_p()
+    rc = L.gapgpu_model_create(x, len(x), b"", str(tmp_path).encode(), ctypes.byref(h))
+    assert rc == _lib.ERR_UNSUPPORTED
+
+
+def test_no_gpu_means_loud_failure(tmp_path):
+    """No CPU fallback: without a GPU, model creation fails with GAPGPU_ERR_CUDA."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    from quip_gb300.potential import Potential
+    from quip_gb300._lib import GapGpuError
+    with pytest.raises(GapGpuError) as ei:
+        Potential(param_filename=os.path.join(ROOT, "tests", "golden", "gap_water", "GAP.xml"))
+    assert ei.value.code == _lib.ERR_CUDA
+
+
+def test_xml_writer_round_trip_through_oracle_reader(tmp_path):
+    rng = np.random.default_rng(0)
+    X = rng.normal(size=(7, 51))
+    desc = models.soap_descriptor_string(3.0, 4, 4, species=(14,))
+    p = models.write_gap_xml(str(tmp_path / "m.xml"),
+                             [dict(desc_str=desc, cov="dot_product", delta=2.0, zeta=3.0, X=X, alpha=np.arange(7.0),
+                                   sc=np.ones(7)),
+                              dict(desc_str="distance_2b cutoff=4.0 Z1=14 Z2=14", cov="ard_se", delta=0.5,
+                                   theta=np.array([1.5]), X=np.linspace(1, 4, 5)[:, None], alpha=np.ones(5),
+                                   sc=np.ones(5))], e0={14: -1.25})
+    d = oracle.read_gap_xml(p)
+    assert d["e0"][14] == -1.25
+    c0, c1 = d["coords"]
+    np.testing.assert_array_equal(c0["X"], X)
+    assert c0["zeta"] == 3.0 and c0["delta"] == 2.0 and c0["cov"] == 2
+    assert c1["cov"] == 1 and c1["theta"][0] == 1.5
+    assert models.soap_dim(4, 4, 1) == c0["D"] == 51
+
+
+def test_structure_generators():
+    at = models.si_diamond(2, rattle=0.0)
+    assert len(at) == 64 and abs(at.volume() - 10.86 ** 3) < 1e-9
+    prim = models.si_primitive()
+    assert len(prim) == 2
+    w = 1.0 / np.linalg.norm(np.linalg.inv(prim.lattice), axis=1)
+    assert w.max() < 5.0  # cutoff larger than the cell
+    b = models.random_binary(400, seed=1)
+    assert abs(len(b) / b.volume() - 0.0961) < 2e-3
+    off, j, sh, d, r = oracle.neighbours(b.positions, b.lattice, [1, 1, 1], 1.6)
+    assert len(r) == 0  # minimum separation holds
+    t = models.random_triclinic(30, rng=np.random.default_rng(2))
+    ang = [np.degrees(np.arccos(t.lattice[:, a] @ t.lattice[:, c] / np.linalg.norm(t.lattice[:, a]) /
+                                np.linalg.norm(t.lattice[:, c]))) for a, c in ((0, 1), (0, 2), (1, 2))]
+    assert all(60 < x < 120 for x in ang)
+
+
+def test_oracle_neighbour_semantics():
+    """QUIP semantics: no minimum image, all images inside the cutoff, strict '<'."""
+    prim = models.si_primitive()
+    off, j, sh, d, r = oracle.neighbours(prim.positions, prim.lattice, [1, 1, 1], 5.0)
+    # brute force over images
+    cnt = 0
+    for a in range(2):
+        for b in range(2):
+            for s in np.ndindex(9, 9, 9):
+                s = np.array(s) - 4
+                v = prim.positions[b] + prim.lattice @ s - prim.positions[a]
+                if (a != b or s.any()) and np.linalg.norm(v) < 5.0:
+                    cnt += 1
+    assert cnt == len(r)
+    assert np.all(r < 5.0)
+    # self images are present
+    assert np.any((j[off[0]:off[1]] == 0))
