@@ -87,7 +87,7 @@ int upload_model(gapgpu_model& m) {
     if ((rc = check_device())) return rc;
     cudaGetDevice(&m.device);
     for (Coordinate& co : m.coords) {
-        co.Dpad = (int)round_up(co.D, 64);
+        co.Dpad = (int)round_up(co.D, 128);
         co.Mpad = (int)round_up(co.M, 128);
         std::vector<double> X((size_t)co.Mpad * co.Dpad, 0.0), coef(co.Mpad, 0.0);
         for (int s = 0; s < co.M; ++s) {
