@@ -48,7 +48,7 @@ def build(verbose=False, extra=()):
         objs = list(ex.map(lambda s: _compile(s, list(extra)), SOURCES))
     if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs):
         return LIB
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcuda"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

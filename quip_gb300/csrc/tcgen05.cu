@@ -16,6 +16,7 @@
 // Every mbarrier wait is bounded; on expiry the kernel records an error code, waits
 // (bounded) for its own work in flight, frees its TMEM and returns.
 #include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cstring>
 #include <cmath>
@@ -338,12 +339,28 @@ float host_tf32(float f) {  // round to nearest, ties away (cvt.rna)
     return r;
 }
 
+// The driver's tensor-map encoder, resolved through the runtime so that the library
+// does not link libcuda directly.
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
 int make_map(CUtensorMap* tm, void* base, CUtensorMapDataType dt, int esize, uint64_t inner, uint64_t outer, uint32_t box_inner) {
+    auto enc = encode_fn();
+    if (!enc) GG_FAIL(GAPGPU_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     cuuint64_t dims[2] = {inner, outer};
     cuuint64_t strides[1] = {inner * (cuuint64_t)esize};
     cuuint32_t box[2] = {box_inner, 128};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = cuTensorMapEncodeTiled(tm, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    CUresult r = enc(tm, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) GG_FAIL(GAPGPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
