@@ -142,11 +142,11 @@ def cpu_reference(w, at, model_path, steps, warmup, sample_atoms=None):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="si4096", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "bf16x3", "tf32"])
+    ap.add_argument("--workload", default="sic32768", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x3", "tf32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -189,35 +189,33 @@ def main():
     at = make_structure(w)
     path = make_model(w, tmp, models.bootstrap_descriptor_fn("fp64"))
     n = len(at)
-    pot = Potential(param_filename=path, precision=args.precision)
-    L = pot._L
-    stream = torch.cuda.current_stream()
-    _lib.check(L.gapgpu_context_set_stream(pot._ctx, _lib.ctypes.c_void_p(stream.cuda_stream)))
-    d_pos = torch.tensor(at.positions, dtype=torch.float64, device="cuda").contiguous()
-    d_Z = torch.tensor(at.numbers, dtype=torch.int32, device="cuda")
-    d_E = torch.zeros(1, dtype=torch.float64, device="cuda")
-    d_F = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
-    d_V = torch.zeros(9, dtype=torch.float64, device="cuda")
     lat = np.asfortranarray(at.lattice).ravel(order="F").copy()
     pbc = np.ones(3, np.int32)
+    stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    d_pos = torch.tensor(at.positions, dtype=torch.float64, device="cuda").contiguous()
+    d_Z = torch.tensor(at.numbers, dtype=torch.int32, device="cuda")
 
-    def step():
-        _lib.check(L.gapgpu_calc_device(pot._ctx, n, d_pos.data_ptr(), d_Z.data_ptr(), _lib.ptr(lat), _lib.ptr(pbc),
-                                        d_E.data_ptr(), d_F.data_ptr(), d_V.data_ptr()))
+    def device_run(pot, steps, warm):
+        L = pot._L
+        _lib.check(L.gapgpu_context_set_stream(pot._ctx, _lib.ctypes.c_void_p(stream.cuda_stream)))
+        d_E = torch.zeros(1, dtype=torch.float64, device="cuda")
+        d_F = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
+        d_V = torch.zeros(9, dtype=torch.float64, device="cuda")
 
-    for _ in range(warmup):
-        step()
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    stage = np.zeros(7)
-    launches = 0
-    clk = Clocks(os.path.join(tmp, "clocks.csv"))
-    with clk:
-        t_wall0 = time.perf_counter()
-        for k in range(args.steps):
+        def step():
+            _lib.check(L.gapgpu_calc_device(pot._ctx, n, d_pos.data_ptr(), d_Z.data_ptr(), _lib.ptr(lat), _lib.ptr(pbc),
+                                            d_E.data_ptr(), d_F.data_ptr(), d_V.data_ptr()))
+
+        for _ in range(warm):
+            step()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        stage = np.zeros(7)
+        launches = 0
+        for k in range(steps):
             flush.zero_()
             evs[k][0].record(stream)
             step()
@@ -225,17 +223,26 @@ def main():
             stage += np.array(list(pot.timings().values()))
             launches += pot.launches()
         torch.cuda.synchronize()
+        ms = [a.elapsed_time(b) for a, b in evs]
+        return dict(t=sum(ms) / 1e3, ms=ms, stage=stage / steps, launches=launches, E=float(d_E.item()),
+                    F=d_F.cpu().numpy(), V=d_V.cpu().numpy().reshape(3, 3, order="F"))
+
+    pot = Potential(param_filename=path, precision=args.precision)
+    clk = Clocks(os.path.join(tmp, "clocks.csv"))
+    with clk:
+        t_wall0 = time.perf_counter()
+        run = device_run(pot, args.steps, warmup)
         t_wall = time.perf_counter() - t_wall0
-    ms = [a.elapsed_time(b) for a, b in evs]
-    t_dev = sum(ms) / 1e3
+    t_dev = run["t"]
     if world > 1:
         t = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_dev = float(t.item())
     value = world * n * args.steps / t_dev
-    stage /= args.steps
+    stage = run["stage"]
 
-    # end to end through the public host API with pinned buffers
+    # end to end through the public host API (gapgpu_calc) with pinned buffers
+    L = pot._L
     pin_pos = torch.tensor(at.positions, dtype=torch.float64).pin_memory()
     pin_Z = torch.tensor(at.numbers, dtype=torch.int32).pin_memory()
     pin_F = torch.zeros((n, 3), dtype=torch.float64).pin_memory()
@@ -257,6 +264,23 @@ def main():
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_value = n * args.steps / (sum(e2e_ms) / 1e3)
 
+    # the plain FP64 path on the same structure: throughput and the mixed path's error
+    fp64 = None
+    if args.precision != "fp64":
+        pot64 = Potential(param_filename=path, precision="fp64")
+        r64 = device_run(pot64, max(1, min(2, args.steps)), 1)
+        fp64 = {"value": n * max(1, min(2, args.steps)) / r64["t"], "unit": "atom-evals/s",
+                "ms_per_step": 1e3 * r64["t"] / max(1, min(2, args.steps)),
+                "stage_ms": dict(zip(["neighbours", "soap_fwd", "gemm", "soap_bwd", "pair2b", "reduce", "total"],
+                                     [round(x, 3) for x in r64["stage"]])),
+                "mixed_speedup": value / (n * max(1, min(2, args.steps)) / r64["t"]),
+                "error_vs_fp64": {"force_max_eV_per_A": float(np.abs(run["F"] - r64["F"]).max()),
+                                  "force_rms_eV_per_A": float(np.sqrt(np.mean((run["F"] - r64["F"]) ** 2))),
+                                  "energy_per_atom_eV": abs(run["E"] - r64["E"]) / n,
+                                  "virial_max_eV": float(np.abs(run["V"] - r64["V"]).max())},
+                "force_max_abs_eV_per_A": float(np.abs(r64["F"]).max())}
+        del pot64
+
     # neighbour statistics for the algorithmic count
     off, j, sh = pot.neighbours(at, w["cutoff"])
     d = at.positions[j] - np.repeat(at.positions, np.diff(off), axis=0) + (at.lattice @ sh.T).T
@@ -266,7 +290,6 @@ def main():
     gemm_ms = stage[2]
     gemm_tflops = n * gemm_atom / (gemm_ms / 1e3) / 1e12 if gemm_ms > 0 else None
     if args.precision == "fp64":
-        # FP64 reference peak: cuBLAS DGEMM through torch (measured now, 4096^3)
         a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
         b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
         for _ in range(2):
@@ -278,23 +301,42 @@ def main():
         e1.record()
         torch.cuda.synchronize()
         peak = 5 * 2 * 4096 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
-        bound, punit, pnote = "fp64", "TFLOP/s", "cuBLAS DGEMM 4096^3 measured in this run"
+        bound, pnote = "fp64", "cuBLAS DGEMM 4096^3 measured in this run"
         del a, b
+        mult = 1.0
     else:
-        peak = pk["bf16_tflops"] / (3.0 if args.precision == "bf16x3" else 2.0)
-        bound, punit, pnote = "tensor", "TFLOP/s", "measured bf16 burst / %s" % ("3 (split-BF16 products)" if args.precision == "bf16x3" else "2 (TF32 rate)")
-    roofline = {"bound": bound, "kernel": "sparse-GP kernel GEMMs (K = Q X^T, G = W X)", "achieved": gemm_tflops,
-                "peak": peak, "unit": punit, "frac": (gemm_tflops / peak) if gemm_tflops else None, "traffic": None,
-                "peak_source": pnote, "gemm_flops_per_atom": gemm_atom}
+        mult = 3.0 if args.precision == "bf16x3" else 2.0
+        peak = pk["bf16_tflops"] / mult
+        bound, pnote = "tensor", "of measured: bf16 burst %.1f TF/s / %g (%s)" % (
+            pk["bf16_tflops"], mult, "3 split-BF16 products" if mult == 3 else "TF32 at half the BF16 rate")
+    roofline = {"bound": bound, "kernel": "sparse-GP kernel GEMMs (k_tc_gemm x2: K = Q X^T with fused kernel epilogue, "
+                                          "G = W X)",
+                "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s",
+                "frac": (gemm_tflops / peak) if gemm_tflops else None, "traffic": None, "peak_source": pnote,
+                "gemm_flops_per_atom": gemm_atom, "gemm_ms_per_step": gemm_ms,
+                "tensor_pipe_flops_per_atom": gemm_atom * mult}
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
-        sample = None if n * w["M"] <= 4096 * 2000 else 256
+        sample = None if n * w["M"] <= 4096 * 2000 else 128
         try:
             cb = cpu_reference(w, at, path, 1, 0, sample)
             cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            if sample:
+                # the mixed result on the same sampled centres against the FP64 oracle
+                from oracle import oracle
+                rng = np.random.default_rng(0)
+                mask = np.zeros(n, np.int32)
+                mask[rng.choice(n, sample, replace=False)] = 1
+                o = oracle.OracleModel.from_xml(path).calc(at.positions, at.numbers, at.lattice, [1, 1, 1], mask=mask,
+                                                           nthreads=os.cpu_count())
+                g = pot.calc(at, atom_mask=mask, local_energy=True)
+                cpu["sampled_error_vs_oracle"] = {
+                    "centres": sample, "force_max_eV_per_A": float(np.abs(g["force"] - o["force"]).max()),
+                    "energy_per_centre_eV": abs(g["energy"] - o["energy"]) / sample,
+                    "virial_max_eV": float(np.abs(g["virial"] - o["virial"]).max())}
         except Exception as e:
-            cpu = {"value": None, "error": str(e)[:120]}
+            cpu = {"value": None, "error": str(e)[:160]}
 
     if rank == 0:
         h2d = n * 3 * 8 + n * 4
@@ -310,10 +352,10 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "stage_ms": dict(zip(["neighbours", "soap_fwd", "gemm", "soap_bwd", "pair2b", "reduce", "total"],
                                      [round(x, 4) for x in stage])),
-                "roofline": roofline, "cpu_baseline": cpu,
+                "fp64": fp64, "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": "atom-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
-                "gpu_launches": int(launches), "clocks": clk.summary(),
+                "gpu_launches": int(run["launches"]), "clocks": clk.summary(),
                 "algorithmic_flops_per_atom": flops_atom, "wall_s": t_wall}
         print(json.dumps(line))
     if world > 1:

@@ -187,7 +187,7 @@ def read_gap_xml(path, label=None):
         scut = np.array([float(s.attrib.get("sparseCutoff", 1.0)) for s in sx])
         M = len(sx)
         if "sparseX_filename" in a:
-            X = np.loadtxt(os.path.join(base, a["sparseX_filename"])).reshape(M, D)
+            X = np.fromfile(os.path.join(base, a["sparseX_filename"]), sep=" ").reshape(M, D)
         else:
             X = np.array([[float(v) for v in (s.text or "").split()] for s in sx]).reshape(M, D)
         theta = None

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <iterator>
 #include <sstream>
 #include <algorithm>
 #include <memory>
@@ -414,14 +415,18 @@ int parse_model(const char* xml, size_t len, const char* init_args, const char* 
         if (gc->attr("sparseX_filename", a)) {
             std::string path = a;
             if (base_dir && *base_dir && !path.empty() && path[0] != '/') path = std::string(base_dir) + "/" + path;
-            std::ifstream f(path);
+            std::ifstream f(path, std::ios::binary);
             if (!f) GG_FAIL(GAPGPU_ERR_XML, "cannot open sparseX file " + path);
-            std::string tok;
+            std::string buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+            for (auto& ch : buf) if (ch == 'd' || ch == 'D') ch = 'e';  // Fortran exponents
+            const char* q = buf.c_str();
             size_t k = 0;
-            double d;
-            while (k < c.X.size() && f >> tok) {
-                if (!to_double(tok, d)) GG_FAIL(GAPGPU_ERR_XML, "bad value in " + path);
+            while (k < c.X.size()) {
+                char* end = nullptr;
+                double d = std::strtod(q, &end);
+                if (end == q) break;
                 c.X[k++] = d;
+                q = end;
             }
             if (k != c.X.size()) GG_FAIL(GAPGPU_ERR_XML, "sparseX file " + path + " holds fewer than M*D values");
         } else {

@@ -164,7 +164,7 @@ def write_gap_xml(path, coords, e0=None, label="GB300_GAP"):
         X = np.asarray(c["X"], dtype=np.float64).reshape(len(c["alpha"]), -1)
         M, D = X.shape
         sname = "%s.sparseX.%s%d" % (fn, label, k + 1)
-        np.savetxt(os.path.join(base, sname), X.reshape(-1), fmt="%.20e")
+        X.reshape(-1).tofile(os.path.join(base, sname), sep="\n", format="%.20e")
         cov = {"ard_se": 1, "dot_product": 2}[c["cov"]]
         zeta = ' zeta="%.17e"' % c["zeta"] if cov == 2 else ""
         out.append('    <gpCoordinates label="%s%d" dimensions="%d" signal_variance="%.17e" signal_mean="0.0" '
