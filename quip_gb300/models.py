@@ -141,6 +141,28 @@ def soap_descriptor_string(cutoff, n_max, l_max, atom_sigma=0.5, width=1.0, spec
                                                             " ".join(map(str, centres))))
 
 
+def parse_descriptor(desc):
+    """key=value pairs of a descriptor string; values may be {..} lists or quoted."""
+    import re
+    out = {}
+    for k, v, bare in re.findall(r'(\S+?)=(\{[^}]*\}|"[^"]*"|\S+)|(\S+)', desc):
+        if bare:
+            out[bare] = True
+        else:
+            out[k] = v[1:-1].strip() if v[:1] in "{\"" else v
+    return out
+
+
+def descriptor_dim(desc):
+    a = parse_descriptor(desc)
+    if "soap" in a:
+        ns = int(a.get("n_species", 1))
+        return soap_dim(int(a.get("n_max", 4)), int(a.get("l_max", 4)), ns)
+    if "distance_2b" in a:
+        return 1
+    raise ValueError("unknown descriptor %r" % desc)
+
+
 def soap_dim(n_max, l_max, n_species):
     N = n_max * n_species
     return (l_max + 1) * N * (N + 1) // 2 + 1
@@ -219,9 +241,7 @@ def bootstrap_descriptor_fn(precision="fp64"):
     def fn(desc, at):
         if desc not in cache:
             d = tempfile.mkdtemp(prefix="gapboot")
-            a = dict(kv.split("=", 1) for kv in desc.split()[1:] if "=" in kv)
-            ns = len(a["species_Z"].strip("{}").split())
-            D = soap_dim(int(a["n_max"]), int(a["l_max"]), ns)
+            D = descriptor_dim(desc)
             p = write_gap_xml(os.path.join(d, "boot.xml"),
                               [dict(desc_str=desc, cov="dot_product", delta=1.0, zeta=1.0,
                                     X=np.eye(1, D), alpha=np.zeros(1), sc=np.ones(1))])

@@ -117,3 +117,12 @@ def test_oracle_neighbour_semantics():
     assert np.all(r < 5.0)
     # self images are present
     assert np.any((j[off[0]:off[1]] == 0))
+
+
+def test_descriptor_string_parsing():
+    d = models.soap_descriptor_string(5.0, 10, 8, species=(14, 6))
+    a = models.parse_descriptor(d)
+    assert a["species_Z"] == "14 6" and a["n_species"] == "2" and a["soap"] is True
+    assert models.descriptor_dim(d) == 1891
+    assert models.descriptor_dim(models.soap_descriptor_string(5.0, 8, 6)) == 253
+    assert models.descriptor_dim("distance_2b cutoff=4 Z1=1 Z2=8") == 1
