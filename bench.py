@@ -148,6 +148,7 @@ def main():
     ap.add_argument("--workload", default="sic32768", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x3", "tf32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-compare", action="store_true", help="skip the FP64 comparison run (profiling)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -266,7 +267,7 @@ def main():
 
     # the plain FP64 path on the same structure: throughput and the mixed path's error
     fp64 = None
-    if args.precision != "fp64":
+    if args.precision != "fp64" and not args.no_fp64_compare:
         pot64 = Potential(param_filename=path, precision="fp64")
         r64 = device_run(pot64, max(1, min(2, args.steps)), 1)
         fp64 = {"value": n * max(1, min(2, args.steps)) / r64["t"], "unit": "atom-evals/s",

@@ -186,7 +186,7 @@ using namespace gapgpu;
 
 gapgpu_context::~gapgpu_context() {
     for (DBuf* b : {&pos, &Z, &mask, &out_e, &out_f, &out_v, &out_le, &out_lv, &cell_key, &cell_key2, &atom_idx, &atom_idx2,
-                    &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev,
+                    &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev, &nbr_i, &wpos,
                     &total, &fpair, &epair, &eatom, &flags, &centres, &ncent, &coef, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf,
                     &Wlo, &epart, &ecent, &Gbuf, &scratch})
         b->release();

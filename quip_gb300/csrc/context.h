@@ -35,7 +35,7 @@ struct gapgpu_context {
     gapgpu::DBuf pos, Z, mask, out_e, out_f, out_v, out_le, out_lv;
     // cells and neighbours
     gapgpu::DBuf cell_key, cell_key2, atom_idx, atom_idx2, cell_start, cell_end, ms, cub_tmp, minmax;
-    gapgpu::DBuf nbr_cnt, nbr_off, nbr_j, nbr_d, nbr_s, nbr_rev, total;
+    gapgpu::DBuf nbr_cnt, nbr_off, nbr_j, nbr_d, nbr_s, nbr_rev, nbr_i, wpos, total;
     // per pair / per atom accumulators
     gapgpu::DBuf fpair, epair, eatom;
     // SOAP / GP workspace

@@ -34,6 +34,9 @@ __device__ __forceinline__ int pack_shift(int a, int b, int c) {
 
 struct GeomDev {
     double lat[9], lat_eff_inv[9], lat_off[3], cutoff;
+    double origin[3];     // Cartesian corner of the effective cell (non-periodic axes)
+    float lat32[9];
+    float lim2;           // (cutoff + margin)^2 for the FP32 pre-filter
     int cellsN[3], img[3], pbc[3];
 };
 
@@ -57,6 +60,19 @@ __global__ void k_assign(int n, const double* __restrict__ pos, GeomDev g, int* 
     idx[a] = a;
 }
 
+// Wrapped positions (pos + L map_shift - origin) in FP32, in cell-sorted order, for the
+// pre-filter: magnitudes stay within the cell, so FP32 rounding is ~1e-7 of the cell size.
+__global__ void k_wrapped(int n, const double* __restrict__ pos, GeomDev g, const int* __restrict__ sorted,
+                          const int* __restrict__ ms, float4* __restrict__ wpos) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int a = sorted[k];
+    double p[3];
+    for (int d = 0; d < 3; ++d)
+        p[d] = pos[3 * a + d] + g.lat[d] * ms[3 * a] + g.lat[3 + d] * ms[3 * a + 1] + g.lat[6 + d] * ms[3 * a + 2] - g.origin[d];
+    wpos[k] = make_float4((float)p[0], (float)p[1], (float)p[2], 0.f);
+}
+
 __global__ void k_cell_ranges(int n, const int* __restrict__ key, int* __restrict__ start, int* __restrict__ end) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -65,12 +81,26 @@ __global__ void k_cell_ranges(int n, const int* __restrict__ key, int* __restric
     if (k == n - 1 || key[k + 1] != c) end[c] = k + 1;
 }
 
-// Visits every candidate (a2, shift) of atom a in the reference's cell-image order.
-template <class F>
-__device__ void scan_images(int a, const double* __restrict__ pos, const GeomDev& g, const int* __restrict__ key_of_atom,
-                            const int* __restrict__ ms, const int* __restrict__ sorted, const int* __restrict__ cstart,
-                            const int* __restrict__ cend, F&& emit) {
-    int lin = key_of_atom[a];
+// One warp per atom (atoms taken in cell order for locality).  The warp walks the
+// atom's image cells in the reference's loop order; lanes take the candidates of a
+// cell 32 at a time, so the emitted order (cell-image order, then position in the
+// sorted cell) is fixed.  A candidate first passes an FP32 test on wrapped
+// coordinates with a safety margin; survivors are decided by the exact FP64 test of
+// test_form_bond (dd = pos_b - pos_a + L shift accumulated without fused multiply-add,
+// kept when sqrt(dd.dd) < cutoff).
+template <bool FILL>
+__global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__ pos, const float4* __restrict__ wpos,
+                                               GeomDev g, const int* __restrict__ key_of_atom, const int* __restrict__ ms,
+                                               const int* __restrict__ sorted, const int* __restrict__ cstart,
+                                               const int* __restrict__ cend, int* __restrict__ cnt,
+                                               const int* __restrict__ off, int* __restrict__ nj, double4* __restrict__ nd,
+                                               int* __restrict__ ns, int* __restrict__ ni, int* __restrict__ bad) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const int a = sorted[warp];
+    const float4 pa32 = wpos[warp];
+    const int lin = key_of_atom[a];
     int cc[3] = {lin % g.cellsN[0], (lin / g.cellsN[0]) % g.cellsN[1], lin / (g.cellsN[0] * g.cellsN[1])};
     int mn[3], mx[3];
     for (int d = 0; d < 3; ++d) {
@@ -83,89 +113,81 @@ __device__ void scan_images(int a, const double* __restrict__ pos, const GeomDev
     }
     const double pa0 = pos[3 * a], pa1 = pos[3 * a + 1], pa2 = pos[3 * a + 2];
     const int msa0 = ms[3 * a], msa1 = ms[3 * a + 1], msa2 = ms[3 * a + 2];
+    int count = 0;
+    const int base = FILL ? off[a] : 0;
+    const unsigned lt = (1u << lane) - 1u;
     for (int k2 = mn[2]; k2 <= mx[2]; ++k2) {
-        int k3 = 0, k4;
         int t = cc[2] + k2;
-        if (g.cellsN[2] > 1) k3 = ((t % g.cellsN[2]) + g.cellsN[2]) % g.cellsN[2];
-        k4 = (t - k3) / g.cellsN[2];
+        int k3 = g.cellsN[2] > 1 ? ((t % g.cellsN[2]) + g.cellsN[2]) % g.cellsN[2] : 0;
+        int k4 = (t - k3) / g.cellsN[2];
         for (int j2 = mn[1]; j2 <= mx[1]; ++j2) {
-            int j3 = 0, j4;
             int u = cc[1] + j2;
-            if (g.cellsN[1] > 1) j3 = ((u % g.cellsN[1]) + g.cellsN[1]) % g.cellsN[1];
-            j4 = (u - j3) / g.cellsN[1];
+            int j3 = g.cellsN[1] > 1 ? ((u % g.cellsN[1]) + g.cellsN[1]) % g.cellsN[1] : 0;
+            int j4 = (u - j3) / g.cellsN[1];
             for (int i2 = mn[0]; i2 <= mx[0]; ++i2) {
-                int i3 = 0, i4;
                 int v = cc[0] + i2;
-                if (g.cellsN[0] > 1) i3 = ((v % g.cellsN[0]) + g.cellsN[0]) % g.cellsN[0];
-                i4 = (v - i3) / g.cellsN[0];
-                int cl = i3 + g.cellsN[0] * (j3 + g.cellsN[1] * k3);
-                bool same_cell = (cl == lin);
-                int e = cend[cl];
-                for (int q = cstart[cl]; q < e; ++q) {
-                    int b = sorted[q];
-                    if (b == a && i4 == 0 && j4 == 0 && k4 == 0 && same_cell) continue;
-                    int s0 = i4 - msa0 + ms[3 * b], s1 = j4 - msa1 + ms[3 * b + 1], s2 = k4 - msa2 + ms[3 * b + 2];
-                    // dd = pos_b - pos_a + lattice . shift, accumulated column by column
-                    // without fused multiply-adds, as test_form_bond does
-                    double d0 = __dsub_rn(pos[3 * b], pa0), d1 = __dsub_rn(pos[3 * b + 1], pa1), d2 = __dsub_rn(pos[3 * b + 2], pa2);
-                    d0 = __dadd_rn(d0, __dmul_rn(g.lat[0], (double)s0)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[1], (double)s0));
-                    d2 = __dadd_rn(d2, __dmul_rn(g.lat[2], (double)s0));
-                    d0 = __dadd_rn(d0, __dmul_rn(g.lat[3], (double)s1)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[4], (double)s1));
-                    d2 = __dadd_rn(d2, __dmul_rn(g.lat[5], (double)s1));
-                    d0 = __dadd_rn(d0, __dmul_rn(g.lat[6], (double)s2)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[7], (double)s2));
-                    d2 = __dadd_rn(d2, __dmul_rn(g.lat[8], (double)s2));
-                    if (d0 > g.cutoff || d1 > g.cutoff || d2 > g.cutoff) continue;
-                    double r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
-                    if (r < g.cutoff) emit(b, s0, s1, s2, d0, d1, d2, r);
+                int i3 = g.cellsN[0] > 1 ? ((v % g.cellsN[0]) + g.cellsN[0]) % g.cellsN[0] : 0;
+                int i4 = (v - i3) / g.cellsN[0];
+                const int cl = i3 + g.cellsN[0] * (j3 + g.cellsN[1] * k3);
+                const bool same_cell = (cl == lin);
+                const float ox = g.lat32[0] * i4 + g.lat32[3] * j4 + g.lat32[6] * k4 - pa32.x;
+                const float oy = g.lat32[1] * i4 + g.lat32[4] * j4 + g.lat32[7] * k4 - pa32.y;
+                const float oz = g.lat32[2] * i4 + g.lat32[5] * j4 + g.lat32[8] * k4 - pa32.z;
+                const int e = cend[cl];
+                for (int q0 = cstart[cl]; q0 < e; q0 += 32) {
+                    const int q = q0 + lane;
+                    bool keep = false;
+                    int b = -1, s0 = 0, s1 = 0, s2 = 0;
+                    double d0 = 0, d1 = 0, d2 = 0, r = 0;
+                    if (q < e) {
+                        b = sorted[q];
+                        const float4 pb = wpos[q];
+                        float fx = pb.x + ox, fy = pb.y + oy, fz = pb.z + oz;
+                        bool self0 = (b == a && i4 == 0 && j4 == 0 && k4 == 0 && same_cell);
+                        if (!self0 && fx * fx + fy * fy + fz * fz < g.lim2) {
+                            s0 = i4 - msa0 + ms[3 * b]; s1 = j4 - msa1 + ms[3 * b + 1]; s2 = k4 - msa2 + ms[3 * b + 2];
+                            d0 = __dsub_rn(pos[3 * b], pa0); d1 = __dsub_rn(pos[3 * b + 1], pa1); d2 = __dsub_rn(pos[3 * b + 2], pa2);
+                            d0 = __dadd_rn(d0, __dmul_rn(g.lat[0], (double)s0)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[1], (double)s0));
+                            d2 = __dadd_rn(d2, __dmul_rn(g.lat[2], (double)s0));
+                            d0 = __dadd_rn(d0, __dmul_rn(g.lat[3], (double)s1)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[4], (double)s1));
+                            d2 = __dadd_rn(d2, __dmul_rn(g.lat[5], (double)s1));
+                            d0 = __dadd_rn(d0, __dmul_rn(g.lat[6], (double)s2)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[7], (double)s2));
+                            d2 = __dadd_rn(d2, __dmul_rn(g.lat[8], (double)s2));
+                            if (!(d0 > g.cutoff || d1 > g.cutoff || d2 > g.cutoff)) {
+                                r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+                                keep = r < g.cutoff;
+                            }
+                        }
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, keep);
+                    if (FILL && keep) {
+                        const int p = base + count + __popc(m & lt);
+                        nj[p] = b;
+                        nd[p] = make_double4(d0, d1, d2, r);
+                        ns[p] = pack_shift(s0, s1, s2);
+                        ni[p] = a;
+                        if (r < 1e-10) atomicOr(bad, 2);
+                    }
+                    count += __popc(m);
                 }
             }
         }
     }
+    if (!FILL && lane == 0) cnt[a] = count;
 }
 
-__global__ void k_count(int n, const double* __restrict__ pos, GeomDev g, const int* __restrict__ key_of_atom,
-                        const int* __restrict__ ms, const int* __restrict__ sorted, const int* __restrict__ cstart,
-                        const int* __restrict__ cend, int* __restrict__ cnt) {
-    int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
-    int c = 0;
-    scan_images(a, pos, g, key_of_atom, ms, sorted, cstart, cend,
-                [&](int, int, int, int, double, double, double, double) { ++c; });
-    cnt[a] = c;
-}
-
-__global__ void k_fill(int n, const double* __restrict__ pos, GeomDev g, const int* __restrict__ key_of_atom,
-                       const int* __restrict__ ms, const int* __restrict__ sorted, const int* __restrict__ cstart,
-                       const int* __restrict__ cend, const int* __restrict__ off, int* __restrict__ nj,
-                       double4* __restrict__ nd, int* __restrict__ ns, int* __restrict__ bad) {
-    int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
-    int p = off[a];
-    scan_images(a, pos, g, key_of_atom, ms, sorted, cstart, cend,
-                [&](int b, int s0, int s1, int s2, double d0, double d1, double d2, double r) {
-                    nj[p] = b;
-                    nd[p] = make_double4(d0, d1, d2, r);
-                    ns[p] = pack_shift(s0, s1, s2);
-                    if (r < 1e-10) atomicOr(bad, 2);
-                    ++p;
-                });
-}
-
-__global__ void k_reverse(int n, const int* __restrict__ off, const int* __restrict__ nj, const int* __restrict__ ns,
-                          int* __restrict__ rev, int* __restrict__ bad) {
-    int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
-    for (int p = off[a]; p < off[a + 1]; ++p) {
-        int b = nj[p];
-        int s = ns[p];
-        int s0 = (s & 1023) - 512, s1 = ((s >> 10) & 1023) - 512, s2 = ((s >> 20) & 1023) - 512;
-        int want = pack_shift(-s0, -s1, -s2);
-        int found = -1;
-        for (int q = off[b]; q < off[b + 1]; ++q)
-            if (nj[q] == a && ns[q] == want) { found = q; break; }
-        rev[p] = found;
-        if (found < 0) atomicOr(bad, 4);
-    }
+__global__ void k_reverse(long long P, const int* __restrict__ off, const int* __restrict__ nj, const int* __restrict__ ni,
+                          const int* __restrict__ ns, int* __restrict__ rev, int* __restrict__ bad) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int a = ni[p], b = nj[p], s = ns[p];
+    const int s0 = (s & 1023) - 512, s1 = ((s >> 10) & 1023) - 512, s2 = ((s >> 20) & 1023) - 512;
+    const int want = pack_shift(-s0, -s1, -s2);
+    int found = -1;
+    for (int q = off[b]; q < off[b + 1]; ++q)
+        if (nj[q] == a && ns[q] == want) { found = q; break; }
+    rev[p] = found;
+    if (found < 0) atomicOr(bad, 4);
 }
 
 void inv3(const double* a, double* g) {
@@ -299,15 +321,28 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
             GG_FAIL(GAPGPU_ERR_ATOMS, "calc_connect: cutoff is too large for the cell (more than 2e6 periodic images)");
     }
     const int ncell = g.cellsN[0] * g.cellsN[1] * g.cellsN[2];
+    // FP32 pre-filter data: origin of the effective cell, FP32 lattice, margin
+    {
+        double bsize = 0;
+        for (int d = 0; d < 3; ++d) {
+            g.origin[d] = lat_eff[d] * g.lat_off[0] + lat_eff[3 + d] * g.lat_off[1] + lat_eff[6 + d] * g.lat_off[2];
+            bsize += norm3(lat_eff + 3 * d);
+        }
+        for (int k = 0; k < 9; ++k) g.lat32[k] = (float)lattice[k];
+        double margin = 1e-3 + 1e-6 * bsize + 1e-6 * cutoff;
+        g.lim2 = (float)((cutoff + margin) * (cutoff + margin));
+    }
     if ((rc = c.cell_key.ensure(sizeof(int) * n)) || (rc = c.cell_key2.ensure(sizeof(int) * n)) ||
         (rc = c.atom_idx.ensure(sizeof(int) * n)) || (rc = c.atom_idx2.ensure(sizeof(int) * n)) ||
         (rc = c.ms.ensure(sizeof(int) * 3 * n)) || (rc = c.cell_start.ensure(sizeof(int) * ncell)) ||
         (rc = c.cell_end.ensure(sizeof(int) * ncell)) || (rc = c.nbr_cnt.ensure(sizeof(int) * (n + 1))) ||
-        (rc = c.nbr_off.ensure(sizeof(int) * (n + 1))) || (rc = c.total.ensure(sizeof(int) * 4)))
+        (rc = c.nbr_off.ensure(sizeof(int) * (n + 1))) || (rc = c.total.ensure(sizeof(int) * 4)) ||
+        (rc = c.wpos.ensure(sizeof(float4) * n)))
         return rc;
     int* bad = c.total.as<int>() + 2;
     GG_CUDA(cudaMemsetAsync(c.total.p, 0, sizeof(int) * 4, st));
     const int TB = 128, nb = (n + TB - 1) / TB;
+    const int nbw = (int)(((long long)n * 32 + TB - 1) / TB);  // one warp per atom
     k_assign<<<nb, TB, 0, st>>>(n, d_pos, g, c.cell_key.as<int>(), c.atom_idx.as<int>(), c.ms.as<int>(), bad);
     // stable sort atoms by cell
     int endbit = 1;
@@ -323,24 +358,31 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
     GG_CUDA(cudaMemsetAsync(c.cell_start.p, 0, sizeof(int) * ncell, st));
     GG_CUDA(cudaMemsetAsync(c.cell_end.p, 0, sizeof(int) * ncell, st));
     k_cell_ranges<<<nb, TB, 0, st>>>(n, c.cell_key2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>());
-    k_count<<<nb, TB, 0, st>>>(n, d_pos, g, c.cell_key.as<int>(), c.ms.as<int>(), c.atom_idx2.as<int>(), c.cell_start.as<int>(),
-                               c.cell_end.as<int>(), c.nbr_cnt.as<int>());
+    k_wrapped<<<nb, TB, 0, st>>>(n, d_pos, g, c.atom_idx2.as<int>(), c.ms.as<int>(), c.wpos.as<float4>());
+    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), g, c.cell_key.as<int>(), c.ms.as<int>(),
+                                       c.atom_idx2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>(),
+                                       c.nbr_cnt.as<int>(), nullptr, nullptr, nullptr, nullptr, nullptr, bad);
     GG_CUDA(cudaMemsetAsync(c.nbr_cnt.as<int>() + n, 0, sizeof(int), st));
     GG_CUDA(cub::DeviceScan::ExclusiveSum(c.cub_tmp.p, tmp2, c.nbr_cnt.as<int>(), c.nbr_off.as<int>(), n + 1, st));
     int tot = 0;
     GG_CUDA(cudaMemcpyAsync(&tot, c.nbr_off.as<int>() + n, sizeof(int), cudaMemcpyDeviceToHost, st));
     GG_CUDA(cudaStreamSynchronize(st));
-    c.launches += 5;
+    c.launches += 6;
     if (tot < 0) GG_FAIL(GAPGPU_ERR_ATOMS, "neighbour list larger than 2^31 entries");
     c.n_pairs = tot;
     size_t P = std::max(tot, 1);
     if ((rc = c.nbr_j.ensure(sizeof(int) * P)) || (rc = c.nbr_d.ensure(sizeof(double4) * P)) ||
-        (rc = c.nbr_s.ensure(sizeof(int) * P)) || (rc = c.nbr_rev.ensure(sizeof(int) * P)))
+        (rc = c.nbr_s.ensure(sizeof(int) * P)) || (rc = c.nbr_rev.ensure(sizeof(int) * P)) ||
+        (rc = c.nbr_i.ensure(sizeof(int) * P)))
         return rc;
-    k_fill<<<nb, TB, 0, st>>>(n, d_pos, g, c.cell_key.as<int>(), c.ms.as<int>(), c.atom_idx2.as<int>(), c.cell_start.as<int>(),
-                              c.cell_end.as<int>(), c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(),
-                              c.nbr_s.as<int>(), bad);
-    k_reverse<<<nb, TB, 0, st>>>(n, c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_s.as<int>(), c.nbr_rev.as<int>(), bad);
+    k_pairs<true><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), g, c.cell_key.as<int>(), c.ms.as<int>(),
+                                      c.atom_idx2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>(), nullptr,
+                                      c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.nbr_s.as<int>(),
+                                      c.nbr_i.as<int>(), bad);
+    if (tot > 0)
+        k_reverse<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(tot, c.nbr_off.as<int>(), c.nbr_j.as<int>(),
+                                                                  c.nbr_i.as<int>(), c.nbr_s.as<int>(), c.nbr_rev.as<int>(),
+                                                                  bad);
     c.launches += 2;
     int flags = 0;
     GG_CUDA(cudaMemcpyAsync(&flags, bad, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -32,36 +32,53 @@ __device__ __forceinline__ void fcut(double r, double rc, double w, double& f, d
     f = 1; df = 0;
 }
 
-__global__ void k_pair_2b(int n, const int* __restrict__ Z, const int* __restrict__ mask, const int* __restrict__ off,
-                          const int* __restrict__ nj, const double4* __restrict__ nd, double rc, double w, int Z1, int Z2,
-                          int M, const double* __restrict__ X, const double* __restrict__ coef, double theta,
+// One thread per canonical directed pair (i < j, or i == j with the shift
+// lexicographically positive).  The reverse pair has the same r (bitwise) and hence the
+// same descriptor value, energy and opposite force, so it is written by the same thread:
+// every fpair/epair slot still has exactly one writer per descriptor.
+template <class R>
+__global__ void k_pair_2b(long long P, const int* __restrict__ Z, const int* __restrict__ mask, const int* __restrict__ ni,
+                          const int* __restrict__ nj, const int* __restrict__ ns, const int* __restrict__ rev,
+                          const double4* __restrict__ nd, double rc, double w, int Z1, int Z2, int M,
+                          const double* __restrict__ X, const double* __restrict__ coef, double theta,
                           double* __restrict__ fpair, double* __restrict__ epair) {
-    int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
-    if (mask && !mask[a]) return;
-    const int za = Z[a];
-    const double it2 = 1.0 / (theta * theta);
-    for (int p = off[a]; p < off[a + 1]; ++p) {
-        double4 d = nd[p];
-        if (d.w >= rc) continue;
-        int zb = Z[nj[p]];
-        bool zi1 = Z1 == 0 || za == Z1, zj2 = Z2 == 0 || zb == Z2, zi2 = Z2 == 0 || za == Z2, zj1 = Z1 == 0 || zb == Z1;
-        if (!((zi1 && zj2) || (zi2 && zj1))) continue;
-        double r = d.w, e = 0, de = 0;
-        for (int s = 0; s < M; ++s) {
-            double t = r - X[s];
-            double k = coef[s] * exp(-0.5 * t * t * it2);
-            e += k;
-            de -= k * t * it2;
-        }
-        double f, df;
-        fcut(r, rc, w, f, df);
-        double g = de * f + e * df;
-        double ir = 1.0 / r;
-        fpair[3 * (size_t)p] += g * d.x * ir;
-        fpair[3 * (size_t)p + 1] += g * d.y * ir;
-        fpair[3 * (size_t)p + 2] += g * d.z * ir;
-        epair[p] += 0.5 * e * f;
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int a = ni[p], b = nj[p];
+    if (a > b) return;
+    if (a == b) {
+        int s = ns[p];
+        int s0 = (s & 1023) - 512, s1 = ((s >> 10) & 1023) - 512, s2 = ((s >> 20) & 1023) - 512;
+        if (!(s0 > 0 || (s0 == 0 && (s1 > 0 || (s1 == 0 && s2 > 0))))) return;
+    }
+    const double4 d = nd[p];
+    if (d.w >= rc) return;
+    const int za = Z[a], zb = Z[b];
+    const bool zi1 = Z1 == 0 || za == Z1, zj2 = Z2 == 0 || zb == Z2, zi2 = Z2 == 0 || za == Z2, zj1 = Z1 == 0 || zb == Z1;
+    if (!((zi1 && zj2) || (zi2 && zj1))) return;
+    const bool ca = !mask || mask[a], cb = !mask || mask[b];
+    if (!ca && !cb) return;
+    const R r = (R)d.w, it2 = (R)(1.0 / (theta * theta));
+    R e = 0, de = 0;
+    for (int s = 0; s < M; ++s) {
+        R t = r - (R)X[s];
+        R k = (R)coef[s] * exp(-(R)0.5 * t * t * it2);
+        e += k;
+        de -= k * t * it2;
+    }
+    double f, df;
+    fcut(d.w, rc, w, f, df);
+    const double g = (double)de * f + (double)e * df;
+    const double ir = 1.0 / d.w;
+    const double fx = g * d.x * ir, fy = g * d.y * ir, fz = g * d.z * ir, h = 0.5 * (double)e * f;
+    if (ca) {
+        fpair[3 * (size_t)p] += fx; fpair[3 * (size_t)p + 1] += fy; fpair[3 * (size_t)p + 2] += fz;
+        epair[p] += h;
+    }
+    if (cb) {
+        const long long q = rev[p];
+        fpair[3 * (size_t)q] -= fx; fpair[3 * (size_t)q + 1] -= fy; fpair[3 * (size_t)q + 2] -= fz;
+        epair[q] += h;
     }
 }
 
@@ -120,12 +137,22 @@ __global__ void k_reduce(int n, const double* __restrict__ le, const double* __r
 }  // namespace
 
 int pair_2b(gapgpu_context& c, const Coordinate& co, int n, const int* d_mask) {
+    (void)n;
     if (co.cov != COV_ARD_SE) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "distance_2b needs the ard_se covariance");
-    const int TB = 128;
-    k_pair_2b<<<(n + TB - 1) / TB, TB, 0, c.stream>>>(n, c.Z.as<int>(), d_mask, c.nbr_off.as<int>(), c.nbr_j.as<int>(),
-                                                     c.nbr_d.as<double4>(), co.d2_rc, co.d2_w, co.d2_Z1, co.d2_Z2, co.M,
-                                                     co.dX64, co.dcoef, co.theta[0], c.fpair.as<double>(),
-                                                     c.epair.as<double>());
+    const long long P = c.n_pairs;
+    if (P == 0) return GAPGPU_OK;
+    const int TB = 256;
+    const unsigned nb = (unsigned)((P + TB - 1) / TB);
+    if (c.precision == GAPGPU_FP64)
+        k_pair_2b<double><<<nb, TB, 0, c.stream>>>(P, c.Z.as<int>(), d_mask, c.nbr_i.as<int>(), c.nbr_j.as<int>(),
+                                                   c.nbr_s.as<int>(), c.nbr_rev.as<int>(), c.nbr_d.as<double4>(), co.d2_rc,
+                                                   co.d2_w, co.d2_Z1, co.d2_Z2, co.M, co.dX64, co.dcoef, co.theta[0],
+                                                   c.fpair.as<double>(), c.epair.as<double>());
+    else
+        k_pair_2b<float><<<nb, TB, 0, c.stream>>>(P, c.Z.as<int>(), d_mask, c.nbr_i.as<int>(), c.nbr_j.as<int>(),
+                                                  c.nbr_s.as<int>(), c.nbr_rev.as<int>(), c.nbr_d.as<double4>(), co.d2_rc,
+                                                  co.d2_w, co.d2_Z1, co.d2_Z2, co.M, co.dX64, co.dcoef, co.theta[0],
+                                                  c.fpair.as<double>(), c.epair.as<double>());
     c.launches++;
     GG_CUDA(cudaGetLastError());
     return GAPGPU_OK;
