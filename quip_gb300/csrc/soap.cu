@@ -176,9 +176,35 @@ __device__ __forceinline__ void decode_pair(int pr, int& ia, int& jb) {
 }
 
 constexpr int FWD_THREADS = 128;
-constexpr int NBC = 16;  // neighbours staged per chunk
+constexpr int TC = 32;  // neighbours staged per chunk (one warp builds the species lists)
 
-// Forward: one block per centre.
+__constant__ unsigned char c_l_of_lm[(MAX_LMAX + 1) * (MAX_LMAX + 1)];
+
+__host__ __device__ __forceinline__ int nmp_of(int nm) { return (nm + 3) & ~3; }
+
+// Per-chunk set-up by warp 0: species channel of each staged neighbour and, per
+// species, the list of staged neighbours in staging order (deterministic).
+__device__ __forceinline__ void build_species_lists(const SoapConst& sc, int base, int cnt, const int* __restrict__ Z,
+                                                    const int* __restrict__ nj, const double4* __restrict__ nd, int* spc,
+                                                    int* lst, int* lcnt) {
+    const int lane = threadIdx.x & 31;
+    int s = -1;
+    if (lane < cnt) {
+        double4 d = nd[base + lane];
+        s = (d.w < sc.rc) ? species_channel(sc, Z[nj[base + lane]]) : -1;
+        spc[lane] = s;
+    }
+    const unsigned lt = (1u << lane) - 1u;
+    for (int k = 0; k < sc.n_species; ++k) {
+        unsigned m = __ballot_sync(0xffffffffu, s == k);
+        if (s == k) lst[k * TC + __popc(m & lt)] = lane;
+        if (lane == 0) lcnt[k] = __popc(m);
+    }
+}
+
+// Forward: one block per centre.  Densities are accumulated in the collocation basis
+// ct[s][lm][a] = sum_j fc rho_l(r_j, r_a) Y_lm(r^_j); the orthonormalising transform
+// c[s][n][lm] = sum_a T_an ct[s][lm][a] is applied once per centre.
 template <class R>
 __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int nc, const int* __restrict__ centres,
                                                                const int* __restrict__ Z, const int* __restrict__ off,
@@ -189,30 +215,28 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int 
     const int ci = blockIdx.x;
     if (ci >= nc) return;
     const int atom = centres[ci];
-    const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, nmL = nm * L;
-    R* cs = reinterpret_cast<R*>(smem_raw);        // ncomp
-    R* Ysm = cs + sc.ncomp;                        // NBC * L2
-    R* tmp = Ysm + NBC * L2;                       // NBC * nm * L   (collocation)
-    R* Rsm = tmp + NBC * nmL;                      // NBC * nm * L   (radial coefficients)
-    R* fcs = Rsm + NBC * nmL;                      // NBC
-    int* spc = reinterpret_cast<int*>(fcs + NBC);  // NBC
+    const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, NMP = nmp_of(nm), NS = sc.n_species;
+    R* ct = reinterpret_cast<R*>(smem_raw);          // NS * L2 * NMP
+    R* cs = ct + NS * L2 * NMP;                       // NS * nm * L2
+    R* Ysm = cs + NS * nm * L2;                       // TC * L2
+    R* Ism = Ysm + TC * L2;                           // TC * L * NMP
+    R* fcs = Ism + TC * L * NMP;                      // TC
+    int* spc = reinterpret_cast<int*>(fcs + TC);      // TC
+    int* lst = spc + TC;                              // NS * TC
+    int* lcnt = lst + NS * TC;                        // NS
     const int tid = threadIdx.x;
-    for (int k = tid; k < sc.ncomp; k += blockDim.x) cs[k] = 0;
+    for (int k = tid; k < NS * L2 * NMP; k += blockDim.x) ct[k] = 0;
     const int p0 = off[atom], p1 = off[atom + 1];
-    for (int base = p0; base < p1; base += NBC) {
-        const int cnt = min(NBC, p1 - base);
+    for (int base = p0; base < p1; base += TC) {
+        const int cnt = min(TC, p1 - base);
         __syncthreads();
-        // per neighbour: species channel, cutoff function
+        if (tid < 32) build_species_lists(sc, base, cnt, Z, nj, nd, spc, lst, lcnt);
         if (tid < cnt) {
-            double4 d = nd[base + tid];
-            int s = (d.w < sc.rc) ? species_channel(sc, Z[nj[base + tid]]) : -1;
-            spc[tid] = s;
             R f, df;
-            cutoff_fn<R>((R)d.w, (R)sc.rc, (R)sc.w, f, df);
+            cutoff_fn<R>((R)nd[base + tid].w, (R)sc.rc, (R)sc.w, f, df);
             fcs[tid] = f;
         }
         __syncthreads();
-        // Y_lm columns: (t, m)
         for (int k = tid; k < cnt * L; k += blockDim.x) {
             int t = k / L, m = k % L;
             if (spc[t] < 0) continue;
@@ -220,60 +244,69 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int 
             R ir = (R)1 / (R)d.w;
             ylm_column<R>(m, L, (R)d.x * ir, (R)d.y * ir, (R)d.z * ir, Ysm + t * L2);
         }
-        // collocation: (t, a)
-        for (int k = tid; k < cnt * nm; k += blockDim.x) {
-            int t = k / nm, a = k % nm;
+        for (int k = tid; k < cnt * NMP; k += blockDim.x) {
+            int t = k / NMP, a = k % NMP;
             if (spc[t] < 0) continue;
-            radial_collocation<R>((R)nd[base + t].w, (R)sc.rb[a], (R)sc.alpha, L, tmp + t * nmL + a * L, nullptr);
+            R* out = Ism + t * L * NMP + a;
+            if (a >= nm) {
+                for (int l = 0; l < L; ++l) out[l * NMP] = 0;
+                continue;
+            }
+            R rho[MAX_LMAX + 1];
+            radial_collocation<R>((R)nd[base + t].w, (R)sc.rb[a], (R)sc.alpha, L, rho, nullptr);
+            const R f = fcs[t];
+            for (int l = 0; l < L; ++l) out[l * NMP] = f * rho[l];
         }
         __syncthreads();
-        // R_nl = fc sum_a T_an rho_al : (t, n, l)
-        for (int k = tid; k < cnt * nmL; k += blockDim.x) {
-            int t = k / nmL, r = k % nmL, n = r / L, l = r % L;
-            if (spc[t] < 0) continue;
-            R acc = 0;
-            for (int a = 0; a < nm; ++a) acc += (R)sc.T[a * nm + n] * tmp[t * nmL + a * L + l];
-            Rsm[t * nmL + n * L + l] = acc * fcs[t];
-        }
-        __syncthreads();
-        // accumulate c[s][n][lm]
-        for (int k = tid; k < sc.ncomp; k += blockDim.x) {
-            int s = k / (nm * L2), r = k % (nm * L2), n = r / L2, lm = r % L2;
-            int l = (int)sqrtf((float)lm);
-            if ((l + 1) * (l + 1) <= lm) ++l;
-            R acc = 0;
-            for (int t = 0; t < cnt; ++t)
-                if (spc[t] == s) acc += Rsm[t * nmL + n * L + l] * Ysm[t * L2 + lm];
-            cs[k] += acc;
+        // ct[s][lm][a..a+3] += sum_{t in species s} Y[t][lm] I[t][l][a..a+3]
+        const int NA4 = NMP / 4;
+        for (int k = tid; k < NS * L2 * NA4; k += blockDim.x) {
+            const int s = k / (L2 * NA4), rem = k % (L2 * NA4), lm = rem / NA4, a4 = rem % NA4;
+            const int l = c_l_of_lm[lm];
+            R a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+            const int nt = lcnt[s];
+            const int* ls = lst + s * TC;
+            for (int q = 0; q < nt; ++q) {
+                const int t = ls[q];
+                const R y = Ysm[t * L2 + lm];
+                const R* iv = Ism + (t * L + l) * NMP + 4 * a4;
+                a0 += y * iv[0]; a1 += y * iv[1]; a2 += y * iv[2]; a3 += y * iv[3];
+            }
+            R* o = ct + (s * L2 + lm) * NMP + 4 * a4;
+            o[0] += a0; o[1] += a1; o[2] += a2; o[3] += a3;
         }
     }
     __syncthreads();
-    // central atom
+    // c[s][n][lm] = sum_a T_an ct[s][lm][a]  (+ central atom at l = 0)
     const int zc = Z[atom];
-    for (int k = tid; k < sc.n_species * nm; k += blockDim.x) {
-        int s = k / nm, n = k % nm;
-        if (sc.centre_all || sc.species_Z[s] == zc || sc.species_Z[s] == 0) cs[(s * nm + n) * L2] += (R)sc.centre_R[n];
+    for (int k = tid; k < NS * nm * L2; k += blockDim.x) {
+        const int s = k / (nm * L2), rem = k % (nm * L2), n = rem / L2, lm = rem % L2;
+        const R* v = ct + (s * L2 + lm) * NMP;
+        R acc = 0;
+        for (int a = 0; a < nm; ++a) acc += (R)sc.T[a * nm + n] * v[a];
+        if (lm == 0 && (sc.centre_all || sc.species_Z[s] == zc || sc.species_Z[s] == 0)) acc += (R)sc.centre_R[n];
+        cs[k] = acc;
     }
     __syncthreads();
     R* cg = c_out + (size_t)ci * sc.ncomp;
     for (int k = tid; k < sc.ncomp; k += blockDim.x) cg[k] = cs[k];
-    // power spectrum (reuse staging area)
+    // power spectrum: one item per (ia, jb) pair, all l
     R* ps = Ysm;
-    const int np = sc.n_pairs * L;
     double ss = 0;
-    for (int k = tid; k < np; k += blockDim.x) {
-        int pr = k / L, l = k % L, ia, jb;
+    for (int pr = tid; pr < sc.n_pairs; pr += blockDim.x) {
+        int ia, jb;
         decode_pair(pr, ia, jb);
-        R v = 0;
-        const R* ca = cs + ia * L2 + l * l;
-        const R* cb = cs + jb * L2 + l * l;
-        for (int m = 0; m < 2 * l + 1; ++m) v += ca[m] * cb[m];
-        R fac = (ia != jb ? (R)1.41421356237309504880 : (R)1) * rsqrt((R)(2 * l + 1));
-        v *= fac;
-        ps[k] = v;
-        ss += (double)v * (double)v;
+        const R* ca = cs + ia * L2;
+        const R* cb = cs + jb * L2;
+        const R off2 = ia != jb ? (R)1.41421356237309504880 : (R)1;
+        for (int l = 0; l < L; ++l) {
+            R v = 0;
+            for (int m = l * l; m < (l + 1) * (l + 1); ++m) v += ca[m] * cb[m];
+            v *= off2 * rsqrt((R)(2 * l + 1));
+            ps[pr * L + l] = v;
+            ss += (double)v * (double)v;
+        }
     }
-    // block reduction of |p|^2 in FP64
     typedef cub::BlockReduce<double, FWD_THREADS> BR;
     __shared__ typename BR::TempStorage tmps;
     double tot = BR(tmps).Sum(ss);
@@ -284,6 +317,7 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int 
     }
     __syncthreads();
     const double inv = sc.normalise ? 1.0 / s_norm : 1.0;
+    const int np = sc.n_pairs * L;
     R* qg = q_out + (size_t)ci * sc.dpad;
     for (int k = tid; k < sc.dpad; k += blockDim.x) {
         R v;
@@ -297,7 +331,12 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int 
 constexpr int BWD_THREADS = 128;
 constexpr int BWD_WARPS = BWD_THREADS / 32;
 
-// Backward: one block per centre; warps take neighbours.
+// Backward: one block per centre.
+//   dE/dp (FP64 normalisation Jacobian) -> H_l[a][b]
+//   dE/dc[a][lm] = sum_b H_l[a][b] c[b][lm]
+//   h[s][lm][a'] = sum_n T_a'n dE/dc[s][n][lm]        (back to the collocation basis)
+//   per pair t of species s:  u_lm = sum_a h[s][lm][a] rho_al(r),  w_lm = sum_a h[s][lm][a] drho_al/dr
+//   f_t = sum_lm [(fc w_lm + fc' u_lm) Y_lm r^ + fc u_lm grad Y_lm]
 template <class R>
 __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, int nc, const int* __restrict__ centres,
                                                                 const int* __restrict__ Z, const int* __restrict__ off,
@@ -309,17 +348,23 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, int
     const int ci = blockIdx.x;
     if (ci >= nc) return;
     const int atom = centres[ci];
-    const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, nmL = nm * L, NN = sc.n_species * nm;
+    const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, NMP = nmp_of(nm), NS = sc.n_species, NN = NS * nm;
     const int np = sc.n_pairs * L;
-    R* cs = reinterpret_cast<R*>(smem_raw);  // ncomp
-    R* dc = cs + sc.ncomp;                   // ncomp (dE/dc)
-    R* dp = dc + sc.ncomp;                   // np    (dE/dp)
-    R* wbase = dp + np;                      // per warp: Y dual (4 L2) + rho (2 nmL) + R (2 nmL)
-    const int per_warp = 4 * L2 + 4 * nmL;
+    R* hs = reinterpret_cast<R*>(smem_raw);            // NS * L2 * NMP
+    R* cs = hs + NS * L2 * NMP;                         // ncomp (c, then dE/dc in place of a copy)
+    R* dc = cs + sc.ncomp;                              // ncomp
+    R* dp = dc + sc.ncomp;                              // np (H values)
+    Dual<R>* Yd = reinterpret_cast<Dual<R>*>(dp + np);  // TC * L2
+    R* Ism = reinterpret_cast<R*>(Yd + TC * L2);        // TC * L * NMP
+    R* dIsm = Ism + TC * L * NMP;                       // TC * L * NMP
+    R* fcs = dIsm + TC * L * NMP;                       // TC
+    R* dfcs = fcs + TC;                                 // TC
+    int* spc = reinterpret_cast<int*>(dfcs + TC);       // TC
+    int* lst = spc + TC;                                // NS * TC (unused order; kept for the shared set-up)
+    int* lcnt = lst + NS * TC;                          // NS
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const R* cg = c_in + (size_t)ci * sc.ncomp;
     for (int k = tid; k < sc.ncomp; k += blockDim.x) cs[k] = cg[k];
-    // dE/dp = (G - q (q.G)) / |p|   (FP64)
     const R* qg = q_in + (size_t)ci * sc.dpad;
     const R* gg = G + (size_t)ci * sc.dpad;
     double qd = 0;
@@ -337,77 +382,100 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, int
         int pr = k / L, ia, jb;
         decode_pair(pr, ia, jb);
         double fac = (ia != jb ? 1.41421356237309504880 : 2.0) / sqrt((double)(2 * l + 1));
-        dp[k] = (R)(v * fac);  // H_l[ia][jb] (= H_l[jb][ia])
+        dp[k] = (R)(v * fac);
     }
     __syncthreads();
-    // dE/dc[a][lm] = sum_b H_l[a][b] c[b][lm]
     for (int k = tid; k < sc.ncomp; k += blockDim.x) {
-        int a = k / L2, lm = k % L2;
-        int l = (int)sqrtf((float)lm);
-        if ((l + 1) * (l + 1) <= lm) ++l;
+        const int a = k / L2, lm = k % L2;
+        const int l = c_l_of_lm[lm];
         R acc = 0;
+        const int rowa = a * (a + 1) / 2;
         for (int b = 0; b < NN; ++b) {
-            int hi = a > b ? a : b, lo = a > b ? b : a;
-            acc += dp[(hi * (hi + 1) / 2 + lo) * L + l] * cs[b * L2 + lm];
+            const int idx = (b <= a ? rowa + b : b * (b + 1) / 2 + a) * L + l;
+            acc += dp[idx] * cs[b * L2 + lm];
         }
         dc[k] = acc;
     }
     __syncthreads();
-    // per-pair contraction
-    R* wY = wbase + wid * per_warp;            // 4*L2  (v, x, y, z interleaved as Dual)
-    R* wrho = wY + 4 * L2;                     // 2*nmL (rho, drho)
-    R* wR = wrho + 2 * nmL;                    // 2*nmL (R, dR)
-    Dual<R>* Yd = reinterpret_cast<Dual<R>*>(wY);
+    for (int k = tid; k < NS * L2 * NMP; k += blockDim.x) {
+        const int s = k / (L2 * NMP), rem = k % (L2 * NMP), lm = rem / NMP, a = rem % NMP;
+        R acc = 0;
+        if (a < nm)
+            for (int n = 0; n < nm; ++n) acc += (R)sc.T[a * nm + n] * dc[(s * nm + n) * L2 + lm];
+        hs[k] = acc;
+    }
     const int p0 = off[atom], p1 = off[atom + 1];
-    for (int p = p0 + wid; p < p1; p += BWD_WARPS) {
-        double4 d = nd[p];
-        int s = (d.w < sc.rc) ? species_channel(sc, Z[nj[p]]) : -1;
-        if (s < 0) continue;  // warp-uniform
-        R r = (R)d.w, ir = (R)1 / r;
-        for (int m = lane; m < L; m += 32) ylm_column_grad<R>(m, L, (R)d.x, (R)d.y, (R)d.z, r, Yd);
-        for (int a = lane; a < nm; a += 32)
-            radial_collocation<R>(r, (R)sc.rb[a], (R)sc.alpha, L, wrho + a * L, wrho + nmL + a * L);
-        __syncwarp();
-        R f, df;
-        cutoff_fn<R>(r, (R)sc.rc, (R)sc.w, f, df);
-        for (int k = lane; k < nmL; k += 32) {
-            int n = k / L, l = k % L;
-            R a0 = 0, a1 = 0;
-            for (int a = 0; a < nm; ++a) {
-                R t = (R)sc.T[a * nm + n];
-                a0 += t * wrho[a * L + l];
-                a1 += t * wrho[nmL + a * L + l];
+    for (int base = p0; base < p1; base += TC) {
+        const int cnt = min(TC, p1 - base);
+        __syncthreads();
+        if (tid < 32) build_species_lists(sc, base, cnt, Z, nj, nd, spc, lst, lcnt);
+        if (tid < cnt) {
+            R f, df;
+            cutoff_fn<R>((R)nd[base + tid].w, (R)sc.rc, (R)sc.w, f, df);
+            fcs[tid] = f;
+            dfcs[tid] = df;
+        }
+        __syncthreads();
+        for (int k = tid; k < cnt * L; k += blockDim.x) {
+            int t = k / L, m = k % L;
+            if (spc[t] < 0) continue;
+            double4 d = nd[base + t];
+            ylm_column_grad<R>(m, L, (R)d.x, (R)d.y, (R)d.z, (R)d.w, Yd + t * L2);
+        }
+        for (int k = tid; k < cnt * NMP; k += blockDim.x) {
+            int t = k / NMP, a = k % NMP;
+            if (spc[t] < 0) continue;
+            R* o = Ism + t * L * NMP + a;
+            R* od = dIsm + t * L * NMP + a;
+            if (a >= nm) {
+                for (int l = 0; l < L; ++l) { o[l * NMP] = 0; od[l * NMP] = 0; }
+                continue;
             }
-            wR[k] = a0 * f;
-            wR[nmL + k] = a1 * f + a0 * df;
+            R rho[MAX_LMAX + 1], drho[MAX_LMAX + 1];
+            radial_collocation<R>((R)nd[base + t].w, (R)sc.rb[a], (R)sc.alpha, L, rho, drho);
+            for (int l = 0; l < L; ++l) { o[l * NMP] = rho[l]; od[l * NMP] = drho[l]; }
         }
-        __syncwarp();
-        R fx = 0, fy = 0, fz = 0;
-        const R ux = (R)d.x * ir, uy = (R)d.y * ir, uz = (R)d.z * ir;
-        const R* dcs = dc + s * nm * L2;
-        for (int k = lane; k < nm * L2; k += 32) {
-            int n = k / L2, lm = k % L2;
-            int l = (int)sqrtf((float)lm);
-            if ((l + 1) * (l + 1) <= lm) ++l;
-            R g = dcs[k];
-            R Rv = wR[n * L + l], dR = wR[nmL + n * L + l];
-            Dual<R> y = Yd[lm];
-            R rad = g * dR * y.v;
-            fx += rad * ux + g * Rv * y.x;
-            fy += rad * uy + g * Rv * y.y;
-            fz += rad * uz + g * Rv * y.z;
+        __syncthreads();
+        const int NA4 = NMP / 4;
+        for (int t = wid; t < cnt; t += BWD_WARPS) {
+            const int s = spc[t];
+            if (s < 0) continue;  // warp-uniform
+            const double4 d = nd[base + t];
+            const R ir = (R)1 / (R)d.w, ux = (R)d.x * ir, uy = (R)d.y * ir, uz = (R)d.z * ir;
+            const R f = fcs[t], df = dfcs[t];
+            R fx = 0, fy = 0, fz = 0;
+            for (int lm = lane; lm < L2; lm += 32) {
+                const int l = c_l_of_lm[lm];
+                const R* hv = hs + (s * L2 + lm) * NMP;
+                const R* iv = Ism + (t * L + l) * NMP;
+                const R* jv = dIsm + (t * L + l) * NMP;
+                R u = 0, w = 0;
+                for (int a4 = 0; a4 < NA4; ++a4) {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const R hh = hv[4 * a4 + e];
+                        u += hh * iv[4 * a4 + e];
+                        w += hh * jv[4 * a4 + e];
+                    }
+                }
+                const Dual<R> y = Yd[t * L2 + lm];
+                const R rad = (f * w + df * u) * y.v, ang = f * u;
+                fx += rad * ux + ang * y.x;
+                fy += rad * uy + ang * y.y;
+                fz += rad * uz + ang * y.z;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                fx += __shfl_xor_sync(0xffffffffu, fx, o);
+                fy += __shfl_xor_sync(0xffffffffu, fy, o);
+                fz += __shfl_xor_sync(0xffffffffu, fz, o);
+            }
+            if (lane == 0) {
+                const size_t p = (size_t)(base + t);
+                fpair[3 * p] += (double)fx;
+                fpair[3 * p + 1] += (double)fy;
+                fpair[3 * p + 2] += (double)fz;
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            fx += __shfl_xor_sync(0xffffffffu, fx, o);
-            fy += __shfl_xor_sync(0xffffffffu, fy, o);
-            fz += __shfl_xor_sync(0xffffffffu, fz, o);
-        }
-        if (lane == 0) {
-            fpair[3 * (size_t)p] += (double)fx;
-            fpair[3 * (size_t)p + 1] += (double)fy;
-            fpair[3 * (size_t)p + 2] += (double)fz;
-        }
-        __syncwarp();
     }
 }
 
@@ -441,21 +509,28 @@ int ensure_ylm_norm() {
             h[l * l + m] = m == 0 ? N : std::sqrt(2.0) * N;
         }
     GG_CUDA(cudaMemcpyToSymbol(c_ylm_norm, h, sizeof h));
+    unsigned char lt[(MAX_LMAX + 1) * (MAX_LMAX + 1)];
+    for (int l = 0; l <= MAX_LMAX; ++l)
+        for (int k = l * l; k < (l + 1) * (l + 1); ++k) lt[k] = (unsigned char)l;
+    GG_CUDA(cudaMemcpyToSymbol(c_l_of_lm, lt, sizeof lt));
     if (dev < 64) g_norm_ready[dev] = true;
     return GAPGPU_OK;
 }
 
 template <class R>
 size_t fwd_smem(const SoapConst& sc) {
-    const int L = sc.l_max + 1, L2 = L * L, nmL = sc.n_max * L;
+    const int L = sc.l_max + 1, L2 = L * L, NMP = nmp_of(sc.n_max), NS = sc.n_species;
+    size_t stage = (size_t)TC * L2 + (size_t)TC * L * NMP + TC;
     size_t ps = (size_t)sc.n_pairs * L;
-    size_t stage = (size_t)NBC * L2 + 2 * (size_t)NBC * nmL + NBC;
-    return sizeof(R) * ((size_t)sc.ncomp + std::max(stage, ps)) + sizeof(int) * NBC + 16;
+    return sizeof(R) * ((size_t)NS * L2 * NMP + (size_t)NS * sc.n_max * L2 + std::max(stage, ps)) +
+           sizeof(int) * (TC + NS * TC + NS) + 64;
 }
 template <class R>
 size_t bwd_smem(const SoapConst& sc) {
-    const int L = sc.l_max + 1, L2 = L * L, nmL = sc.n_max * L;
-    return sizeof(R) * (2 * (size_t)sc.ncomp + (size_t)sc.n_pairs * L + BWD_WARPS * (4 * (size_t)L2 + 4 * (size_t)nmL)) + 16;
+    const int L = sc.l_max + 1, L2 = L * L, NMP = nmp_of(sc.n_max), NS = sc.n_species;
+    return sizeof(R) * ((size_t)NS * L2 * NMP + 2 * (size_t)sc.ncomp + (size_t)sc.n_pairs * L + 4 * (size_t)TC * L2 +
+                        2 * (size_t)TC * L * NMP + 2 * TC) +
+           sizeof(int) * (TC + NS * TC + NS) + 64;
 }
 
 template <class R>
