@@ -112,6 +112,38 @@ int gapgpu_neighbours(gapgpu_context* ctx, int n, const double* pos, const doubl
                       double cutoff, int32_t* offsets, int32_t* nbr_j, int32_t* nbr_shift, int64_t capacity,
                       int64_t* total);
 
+/* Largest structure gapgpu_neighbours_static accepts. */
+#define GAPGPU_STATIC_MAX_ATOMS 65536
+
+/* gapgpu_neighbours_static: the neighbour list of gapgpu_neighbours for callers that
+ * cannot allocate GPU memory.  It has no counterpart in the reference.
+ *
+ * Who needs it: host codes whose device memory all belongs to their own pool allocator
+ * (an MD engine's memory space, a framework that reserves most of HBM at start-up), and
+ * time-step loops that must not call cudaMalloc/cudaFree, which synchronise the device
+ * and stall the host code's other streams.  This entry point makes no allocation:
+ * no cudaMalloc, no cudaFree and no allocating library routine.  Its scratch lives in one
+ * fixed device array of about 9 MiB, which every GPU that loads the library holds until
+ * the process exits.
+ *
+ * The caller owns every input and output, all device pointers except lattice, pbc and
+ * total: d_pos double[3n] (Fortran pos(3,N)), d_offsets int32[n+1], d_nbr_j
+ * int32[capacity], d_nbr_shift int32[3*capacity] (same layout as gapgpu_neighbours).
+ * *total receives the number of entries; when capacity < *total, or d_nbr_j or
+ * d_nbr_shift is NULL, only d_offsets and *total are written.  The work runs on
+ * cuda_stream (NULL = the legacy default stream), and the call waits for that stream
+ * before it returns.
+ *
+ * Limits: n <= GAPGPU_STATIC_MAX_ATOMS (GAPGPU_ERR_ARG above it).  The scratch array is
+ * shared by every call in the process and keeps the previous call's contents, so calls
+ * that overlap on the GPU (other host threads, other streams) race: serialise them.
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress), with that device current; make that first call before any
+ * stream capture begins. */
+int gapgpu_neighbours_static(int n, const double* d_pos, const double* lattice, const int32_t* pbc, double cutoff,
+                             int32_t* d_offsets, int32_t* d_nbr_j, int32_t* d_nbr_shift, int64_t capacity,
+                             int64_t* total, void* cuda_stream);
+
 /* SOAP descriptors (and the sum of squares before normalisation) of every centre
  * for coordinate `coordinate` of the model: the descriptor-only path of
  * quippy/quippy/descriptors.py:165-235.  q: n_centres*dim row-major. */

@@ -18,7 +18,7 @@ PRECISIONS = {"fp64": FP64, "bf16x3": MIXED_BF16X3, "tf32": MIXED_TF32}
 EXPORTS = ["gapgpu_last_error", "gapgpu_model_create", "gapgpu_model_cutoff", "gapgpu_model_info",
            "gapgpu_model_destroy", "gapgpu_context_create", "gapgpu_context_set_stream", "gapgpu_context_destroy",
            "gapgpu_calc", "gapgpu_calc_device", "gapgpu_context_sync", "gapgpu_neighbours", "gapgpu_descriptors",
-           "gapgpu_context_timings", "gapgpu_context_launches"]
+           "gapgpu_context_timings", "gapgpu_context_launches", "gapgpu_neighbours_static"]
 
 
 class GapGpuError(RuntimeError):
@@ -60,6 +60,8 @@ def load(build_if_missing=True):
                                      c_void_p]
     L.gapgpu_neighbours.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
                                     c_void_p, i64, P(i64)]
+    L.gapgpu_neighbours_static.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p, c_void_p,
+                                           i64, P(i64), c_void_p]
     L.gapgpu_descriptors.argtypes = [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, i64,
                                      P(c_int)]
     L.gapgpu_context_timings.argtypes = [c_void_p, P(c_double), c_int]

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <algorithm>
+#include <mutex>
 
 #include "context.h"
 
@@ -88,7 +89,9 @@ __global__ void k_cell_ranges(int n, const int* __restrict__ key, int* __restric
 // coordinates with a safety margin; survivors are decided by the exact FP64 test of
 // test_form_bond (dd = pos_b - pos_a + L shift accumulated without fused multiply-add,
 // kept when sqrt(dd.dd) < cutoff).
-template <bool FILL>
+// CALLER_LAYOUT (fill only): write just j and the unpacked shift (3 ints per entry)
+// into caller-owned arrays, the layout of gapgpu_neighbours; nd/ni are not written.
+template <bool FILL, bool CALLER_LAYOUT = false>
 __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__ pos, const float4* __restrict__ wpos,
                                                GeomDev g, const int* __restrict__ key_of_atom, const int* __restrict__ ms,
                                                const int* __restrict__ sorted, const int* __restrict__ cstart,
@@ -163,9 +166,15 @@ __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__
                     if (FILL && keep) {
                         const int p = base + count + __popc(m & lt);
                         nj[p] = b;
-                        nd[p] = make_double4(d0, d1, d2, r);
-                        ns[p] = pack_shift(s0, s1, s2);
-                        ni[p] = a;
+                        if (CALLER_LAYOUT) {
+                            ns[3 * (size_t)p] = s0;
+                            ns[3 * (size_t)p + 1] = s1;
+                            ns[3 * (size_t)p + 2] = s2;
+                        } else {
+                            nd[p] = make_double4(d0, d1, d2, r);
+                            ns[p] = pack_shift(s0, s1, s2);
+                            ni[p] = a;
+                        }
                         if (r < 1e-10) atomicOr(bad, 2);
                     }
                     count += __popc(m);
@@ -251,11 +260,13 @@ void DBuf::release() {
     cap = 0;
 }
 
-int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double* lattice, const int* pbc, double cutoff,
-                     const int*) {
+// Host set-up of connection_calc_connect for one call: effective lattice of clusters
+// and mixed boundary conditions (calc_lat_eff), cell grid (divide_cell), image ranges
+// (fit_box_in_cell) and the FP32 pre-filter constants.  d_minmax is 6 doubles of device
+// scratch, used only when an axis is not periodic.
+static int neighbour_geometry(int n, const double* d_pos, const double* lattice, const int* pbc, double cutoff, double* d_minmax,
+                       cudaStream_t st, GeomDev& g, long long& launches) {
     if (!(cutoff >= 0.0)) GG_FAIL(GAPGPU_ERR_ATOMS, "calc_connect: negative cutoff radius");
-    cudaStream_t st = c.stream;
-    GeomDev g;
     std::memset(&g, 0, sizeof g);
     std::memcpy(g.lat, lattice, sizeof g.lat);
     g.cutoff = cutoff;
@@ -266,13 +277,11 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
     double lat_eff[9];
     std::memcpy(lat_eff, lattice, sizeof lat_eff);
     std::memcpy(g.lat_eff_inv, gi, sizeof gi);
-    int rc;
     if (!g.pbc[0] || !g.pbc[1] || !g.pbc[2]) {  // calc_lat_eff (Connection.f95:740-763)
-        if ((rc = c.minmax.ensure(6 * sizeof(double)))) return rc;
-        k_latpos_minmax<<<1, 256, 0, st>>>(n, d_pos, g, c.minmax.as<double>());
-        c.launches++;
+        k_latpos_minmax<<<1, 256, 0, st>>>(n, d_pos, g, d_minmax);
+        launches++;
         double mm[6];
-        GG_CUDA(cudaMemcpyAsync(mm, c.minmax.p, sizeof mm, cudaMemcpyDeviceToHost, st));
+        GG_CUDA(cudaMemcpyAsync(mm, d_minmax, sizeof mm, cudaMemcpyDeviceToHost, st));
         GG_CUDA(cudaStreamSynchronize(st));
         for (int d = 0; d < 3; ++d) {
             if (g.pbc[d]) continue;
@@ -320,7 +329,6 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
         if ((long long)(2 * g.img[0] + 1) * (2 * g.img[1] + 1) * (2 * g.img[2] + 1) > 2000000LL)
             GG_FAIL(GAPGPU_ERR_ATOMS, "calc_connect: cutoff is too large for the cell (more than 2e6 periodic images)");
     }
-    const int ncell = g.cellsN[0] * g.cellsN[1] * g.cellsN[2];
     // FP32 pre-filter data: origin of the effective cell, FP32 lattice, margin
     {
         double bsize = 0;
@@ -332,6 +340,18 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
         double margin = 1e-3 + 1e-6 * bsize + 1e-6 * cutoff;
         g.lim2 = (float)((cutoff + margin) * (cutoff + margin));
     }
+    return GAPGPU_OK;
+}
+
+int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double* lattice, const int* pbc, double cutoff,
+                     const int*) {
+    cudaStream_t st = c.stream;
+    GeomDev g;
+    int rc;
+    if ((rc = c.minmax.ensure(6 * sizeof(double))) ||
+        (rc = neighbour_geometry(n, d_pos, lattice, pbc, cutoff, c.minmax.as<double>(), st, g, c.launches)))
+        return rc;
+    const int ncell = g.cellsN[0] * g.cellsN[1] * g.cellsN[2];
     if ((rc = c.cell_key.ensure(sizeof(int) * n)) || (rc = c.cell_key2.ensure(sizeof(int) * n)) ||
         (rc = c.atom_idx.ensure(sizeof(int) * n)) || (rc = c.atom_idx2.ensure(sizeof(int) * n)) ||
         (rc = c.ms.ensure(sizeof(int) * 3 * n)) || (rc = c.cell_start.ensure(sizeof(int) * ncell)) ||
@@ -394,3 +414,136 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
 }
 
 }  // namespace gapgpu
+
+// ---------------------------------------------------------------------------------
+// gapgpu_neighbours_static: the same neighbour build with every piece of scratch in one
+// file-scope device array instead of cudaMalloc'ed buffers.
+//
+// Layout of the array (byte offsets, each 256-byte aligned), for n <= MAX atoms:
+//   key, key2, idx, idx2    int[MAX] each     cell key / atom index before and after the sort
+//   ms                      int[3 MAX]        map_shift of each atom
+//   cnt                     int[MAX + 1]      per-atom pair counts (scanned into the caller's offsets)
+//   cstart, cend            int[MAX_CELLS]    atom range of each cell
+//   wpos                    float4[MAX]       wrapped FP32 positions in cell order
+//   minmax                  double[6]         fractional extent (non-periodic axes)
+//   flags                   int[4]            error bits of the kernels
+//   cub                     bytes             temporary storage of the radix sort and the scan
+namespace gapgpu {
+namespace {
+
+constexpr int STATIC_MAX_ATOMS = GAPGPU_STATIC_MAX_ATOMS;
+constexpr int STATIC_MAX_CELLS = 4 * STATIC_MAX_ATOMS + 64;  // build_neighbours caps cells at 4 n + 64
+constexpr size_t STATIC_CUB_BYTES = size_t(4) << 20;
+
+constexpr size_t al256(size_t v) { return (v + 255) / 256 * 256; }
+constexpr size_t SO_KEY = 0;
+constexpr size_t SO_KEY2 = SO_KEY + al256(sizeof(int) * STATIC_MAX_ATOMS);
+constexpr size_t SO_IDX = SO_KEY2 + al256(sizeof(int) * STATIC_MAX_ATOMS);
+constexpr size_t SO_IDX2 = SO_IDX + al256(sizeof(int) * STATIC_MAX_ATOMS);
+constexpr size_t SO_MS = SO_IDX2 + al256(sizeof(int) * STATIC_MAX_ATOMS);
+constexpr size_t SO_CNT = SO_MS + al256(sizeof(int) * 3 * STATIC_MAX_ATOMS);
+constexpr size_t SO_CSTART = SO_CNT + al256(sizeof(int) * (STATIC_MAX_ATOMS + 1));
+constexpr size_t SO_CEND = SO_CSTART + al256(sizeof(int) * STATIC_MAX_CELLS);
+constexpr size_t SO_WPOS = SO_CEND + al256(sizeof(int) * STATIC_MAX_CELLS);
+constexpr size_t SO_MINMAX = SO_WPOS + al256(sizeof(float4) * STATIC_MAX_ATOMS);
+constexpr size_t SO_FLAGS = SO_MINMAX + al256(sizeof(double) * 6);
+constexpr size_t SO_CUB = SO_FLAGS + al256(sizeof(int) * 4);
+constexpr size_t STATIC_SCRATCH_BYTES = SO_CUB + STATIC_CUB_BYTES;
+
+// Held by every GPU that loads the library, until the process exits.
+static __device__ __align__(256) unsigned char g_nbr_scratch[STATIC_SCRATCH_BYTES];
+
+// Device address of g_nbr_scratch per device.  In host code the symbol name is only a
+// host-side stand-in, so the address is looked up once per device, with that device
+// current, and passed to the kernels.
+std::mutex g_static_mu;
+unsigned char* g_static_addr[64] = {};
+
+int static_scratch(int dev, unsigned char** out) {
+    if (dev < 0 || dev >= 64) GG_FAIL(GAPGPU_ERR_CUDA, "gapgpu_neighbours_static: device ordinal above 63");
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_addr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_nbr_scratch);
+        if (e != cudaSuccess || !ptr)
+            GG_FAIL(GAPGPU_ERR_CUDA, std::string("gapgpu_neighbours_static: cudaGetSymbolAddress failed: ") +
+                                         cudaGetErrorString(e));
+        g_static_addr[dev] = static_cast<unsigned char*>(ptr);
+    }
+    *out = g_static_addr[dev];
+    return GAPGPU_OK;
+}
+
+}  // namespace
+}  // namespace gapgpu
+
+extern "C" int gapgpu_neighbours_static(int n, const double* d_pos, const double* lattice, const int32_t* pbc,
+                                        double cutoff, int32_t* d_offsets, int32_t* d_nbr_j, int32_t* d_nbr_shift,
+                                        int64_t capacity, int64_t* total, void* cuda_stream) {
+    using namespace gapgpu;
+    if (n <= 0 || !d_pos || !lattice || !pbc || !d_offsets || !total)
+        GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_neighbours_static: bad argument");
+    if (n > STATIC_MAX_ATOMS)
+        GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_neighbours_static: " + std::to_string(n) + " atoms is above the static limit of " +
+                                    std::to_string(STATIC_MAX_ATOMS) + " (use gapgpu_neighbours)");
+    int dev = 0;
+    GG_CUDA(cudaGetDevice(&dev));
+    unsigned char* base = nullptr;
+    int rc;
+    if ((rc = static_scratch(dev, &base))) return rc;
+    int* key = reinterpret_cast<int*>(base + SO_KEY);
+    int* key2 = reinterpret_cast<int*>(base + SO_KEY2);
+    int* idx = reinterpret_cast<int*>(base + SO_IDX);
+    int* idx2 = reinterpret_cast<int*>(base + SO_IDX2);
+    int* ms = reinterpret_cast<int*>(base + SO_MS);
+    int* cnt = reinterpret_cast<int*>(base + SO_CNT);
+    int* cstart = reinterpret_cast<int*>(base + SO_CSTART);
+    int* cend = reinterpret_cast<int*>(base + SO_CEND);
+    float4* wpos = reinterpret_cast<float4*>(base + SO_WPOS);
+    double* minmax = reinterpret_cast<double*>(base + SO_MINMAX);
+    int* bad = reinterpret_cast<int*>(base + SO_FLAGS);
+    void* cub_tmp = base + SO_CUB;
+
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    long long launches = 0;
+    GeomDev g;
+    if ((rc = neighbour_geometry(n, d_pos, lattice, pbc, cutoff, minmax, st, g, launches))) return rc;
+    const int ncell = g.cellsN[0] * g.cellsN[1] * g.cellsN[2];
+    if (ncell > STATIC_MAX_CELLS) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_neighbours_static: cell grid above the static limit");
+    int endbit = 1;
+    while ((1 << endbit) < ncell && endbit < 31) ++endbit;
+    size_t t_sort = 0, t_scan = 0;
+    GG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, t_sort, key, key2, idx, idx2, n, 0, endbit, st));
+    GG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, t_scan, cnt, d_offsets, n + 1, st));
+    if (std::max(t_sort, t_scan) > STATIC_CUB_BYTES)
+        GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_neighbours_static: sort workspace above the static limit");
+    // The array keeps the previous call's contents: clear what the kernels accumulate into.
+    GG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int) * 4, st));
+    GG_CUDA(cudaMemsetAsync(cstart, 0, sizeof(int) * ncell, st));
+    GG_CUDA(cudaMemsetAsync(cend, 0, sizeof(int) * ncell, st));
+    GG_CUDA(cudaMemsetAsync(cnt + n, 0, sizeof(int), st));
+    const int TB = 128, nb = (n + TB - 1) / TB;
+    const int nbw = (int)(((long long)n * 32 + TB - 1) / TB);
+    k_assign<<<nb, TB, 0, st>>>(n, d_pos, g, key, idx, ms, bad);
+    GG_CUDA(cub::DeviceRadixSort::SortPairs(cub_tmp, t_sort, key, key2, idx, idx2, n, 0, endbit, st));
+    k_cell_ranges<<<nb, TB, 0, st>>>(n, key2, cstart, cend);
+    k_wrapped<<<nb, TB, 0, st>>>(n, d_pos, g, idx2, ms, wpos);
+    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, wpos, g, key, ms, idx2, cstart, cend, cnt, nullptr, nullptr, nullptr,
+                                       nullptr, nullptr, bad);
+    GG_CUDA(cub::DeviceScan::ExclusiveSum(cub_tmp, t_scan, cnt, d_offsets, n + 1, st));
+    int tot = 0;
+    GG_CUDA(cudaMemcpyAsync(&tot, d_offsets + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GG_CUDA(cudaStreamSynchronize(st));
+    if (tot < 0) GG_FAIL(GAPGPU_ERR_ATOMS, "neighbour list larger than 2^31 entries");
+    *total = tot;
+    if (tot > 0 && capacity >= tot && d_nbr_j && d_nbr_shift)
+        k_pairs<true, true><<<nbw, TB, 0, st>>>(n, d_pos, wpos, g, key, ms, idx2, cstart, cend, nullptr, d_offsets, d_nbr_j,
+                                                nullptr, d_nbr_shift, nullptr, bad);
+    int flags = 0;
+    GG_CUDA(cudaMemcpyAsync(&flags, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GG_CUDA(cudaStreamSynchronize(st));
+    GG_CUDA(cudaGetLastError());
+    if (flags & 1) GG_FAIL(GAPGPU_ERR_ATOMS, "atom positions contain NaN or Inf");
+    if (flags & 2) GG_FAIL(GAPGPU_ERR_ATOMS, "overlapping atoms: a neighbour distance is below 1e-10 (Connection.f95:1394-1398)");
+    return GAPGPU_OK;
+}
