@@ -7,6 +7,7 @@ kernel GEMMs, forces, virial) of one structure of the chosen workload:
   sic32768 32768-atom random Si/C cell (50/50, 3.2 g/cm^3, 1.6 A minimum separation);
            SOAP n_max=10 l_max=8 rc=5 A with 2 species channels (D=1891), 8000 sparse
            points, zeta=4, + distance_2b per species pair.
+  sic8192  the same model on an 8192-atom cell (the size used for ncu captures).
 Inputs are seeded synthetic structures and random GAP models (no dataset is published
 for this path).  `value` is timed with CUDA events on the launching stream with the
 inputs resident in HBM; `e2e` goes through the public C ABI (gapgpu_calc) with pinned
@@ -41,6 +42,8 @@ WORKLOADS = {
     "si4096": dict(kind="si", n_rep=8, rattle=0.1, n_max=8, l_max=6, cutoff=5.0, M=2000, species=(14,), seed=11),
     "si64": dict(kind="si", n_rep=2, rattle=0.05, n_max=8, l_max=6, cutoff=5.0, M=500, species=(14,), seed=7),
     "sic32768": dict(kind="sic", n=32768, n_max=10, l_max=8, cutoff=5.0, M=8000, species=(14, 6), seed=21),
+    # the sic32768 model on an 8192-atom cell: the profiling case (per-kernel inputs still above L2)
+    "sic8192": dict(kind="sic", n=8192, n_max=10, l_max=8, cutoff=5.0, M=8000, species=(14, 6), seed=21),
 }
 
 
