@@ -101,6 +101,10 @@ int upload_model(gapgpu_model& m) {
         GG_CUDA(cudaMemcpy(co.dX64, X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice));
         GG_CUDA(cudaMalloc(&co.dcoef, sizeof(double) * coef.size()));
         GG_CUDA(cudaMemcpy(co.dcoef, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice));
+        if (co.type == DESC_SOAP) {
+            int rc2;
+            if ((rc2 = upload_soap_tables(co))) return rc2;
+        }
     }
     return GAPGPU_OK;
 }
@@ -108,8 +112,9 @@ int upload_model(gapgpu_model& m) {
 void free_model_device(gapgpu_model& m) {
     for (Coordinate& co : m.coords) {
         for (void* p : {(void*)co.dX64, (void*)co.dcoef, (void*)co.dXf32, (void*)co.dXhi, (void*)co.dXlo, (void*)co.dXTf32,
-                        (void*)co.dXThi, (void*)co.dXTlo, (void*)co.dcoef32, (void*)co.dtheta})
+                        (void*)co.dXThi, (void*)co.dXTlo, (void*)co.dcoef32, (void*)co.dtheta, co.dtab[0], co.dtab[1]})
             if (p) cudaFree(p);
+        co.dtab[0] = co.dtab[1] = nullptr;
         co.dX64 = nullptr; co.dcoef = nullptr; co.dXf32 = nullptr; co.dXhi = nullptr; co.dXlo = nullptr;
         co.dXTf32 = nullptr; co.dXThi = nullptr; co.dXTlo = nullptr; co.dcoef32 = nullptr; co.dtheta = nullptr;
     }
@@ -187,7 +192,7 @@ using namespace gapgpu;
 gapgpu_context::~gapgpu_context() {
     for (DBuf* b : {&pos, &Z, &mask, &out_e, &out_f, &out_v, &out_le, &out_lv, &cell_key, &cell_key2, &atom_idx, &atom_idx2,
                     &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev, &nbr_i, &wpos,
-                    &total, &fpair, &epair, &eatom, &flags, &centres, &ncent, &coef, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf,
+                    &total, &fpair, &epair, &eatom, &redpart, &flags, &centres, &ncent, &coef, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf,
                     &Wlo, &epart, &ecent, &Gbuf, &scratch})
         b->release();
     if (events)

@@ -37,7 +37,7 @@ struct gapgpu_context {
     gapgpu::DBuf cell_key, cell_key2, atom_idx, atom_idx2, cell_start, cell_end, ms, cub_tmp, minmax;
     gapgpu::DBuf nbr_cnt, nbr_off, nbr_j, nbr_d, nbr_s, nbr_rev, nbr_i, wpos, total;
     // per pair / per atom accumulators
-    gapgpu::DBuf fpair, epair, eatom;
+    gapgpu::DBuf fpair, epair, eatom, redpart;
     // SOAP / GP workspace
     gapgpu::DBuf flags, centres, ncent, coef, qbuf, qlo, pnorm, Kbuf, Wbuf, Wlo, epart, ecent, Gbuf, scratch;
     // last results

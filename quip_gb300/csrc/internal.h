@@ -81,6 +81,7 @@ struct Coordinate {
     uint16_t* dXTlo = nullptr;
     float* dcoef32 = nullptr;
     double* dtheta = nullptr;   // distance_2b
+    void* dtab[2] = {nullptr, nullptr};  // SOAP constant block (soap_tab layout): [0] FP64, [1] FP32
 };
 
 }  // namespace gapgpu
@@ -103,4 +104,6 @@ void free_model_device(gapgpu_model& m);
 std::map<std::string, std::string> parse_args(const std::string& s);
 void soap_setup(SoapParams& s);
 SoapConst soap_const(const Coordinate& c);
+// soap.cu
+int upload_soap_tables(Coordinate& co);
 }  // namespace gapgpu

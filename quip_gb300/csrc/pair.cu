@@ -20,13 +20,19 @@
 namespace gapgpu {
 namespace {
 
-__device__ __forceinline__ void fcut(double r, double rc, double w, double& f, double& df) {
+__device__ __forceinline__ double fcos(double x) { return cos(x); }
+__device__ __forceinline__ float fcos(float x) { return cosf(x); }
+__device__ __forceinline__ double fsin(double x) { return sin(x); }
+__device__ __forceinline__ float fsin(float x) { return sinf(x); }
+
+template <class R>
+__device__ __forceinline__ void fcut(R r, R rc, R w, R& f, R& df) {
     if (r > rc) { f = 0; df = 0; return; }
     if (r > rc - w) {
-        const double pi = 3.14159265358979323846;
-        double a = pi * (r - rc + w) / w;
-        f = 0.5 * (cos(a) + 1.0);
-        df = -0.5 * pi * sin(a) / w;
+        const R pi = (R)3.14159265358979323846;
+        R a = pi * (r - rc + w) / w;
+        f = (R)0.5 * (fcos(a) + (R)1);
+        df = -(R)0.5 * pi * fsin(a) / w;
         return;
     }
     f = 1; df = 0;
@@ -40,7 +46,7 @@ template <class R>
 __global__ void k_pair_2b(long long P, const int* __restrict__ Z, const int* __restrict__ mask, const int* __restrict__ ni,
                           const int* __restrict__ nj, const int* __restrict__ ns, const int* __restrict__ rev,
                           const double4* __restrict__ nd, double rc, double w, int Z1, int Z2, int M,
-                          const double* __restrict__ X, const double* __restrict__ coef, double theta,
+                          const R* __restrict__ X, const R* __restrict__ coef, double theta,
                           double* __restrict__ fpair, double* __restrict__ epair) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (p >= P) return;
@@ -58,19 +64,21 @@ __global__ void k_pair_2b(long long P, const int* __restrict__ Z, const int* __r
     if (!((zi1 && zj2) || (zi2 && zj1))) return;
     const bool ca = !mask || mask[a], cb = !mask || mask[b];
     if (!ca && !cb) return;
+    // FP64 path: every step in double; mixed path: FP32 GP sum and force, FP64 accumulation.
     const R r = (R)d.w, it2 = (R)(1.0 / (theta * theta));
     R e = 0, de = 0;
     for (int s = 0; s < M; ++s) {
-        R t = r - (R)X[s];
-        R k = (R)coef[s] * exp(-(R)0.5 * t * t * it2);
+        R t = r - X[s];
+        R k = coef[s] * exp(-(R)0.5 * t * t * it2);
         e += k;
         de -= k * t * it2;
     }
-    double f, df;
-    fcut(d.w, rc, w, f, df);
-    const double g = (double)de * f + (double)e * df;
-    const double ir = 1.0 / d.w;
-    const double fx = g * d.x * ir, fy = g * d.y * ir, fz = g * d.z * ir, h = 0.5 * (double)e * f;
+    R f, df;
+    fcut<R>(r, (R)rc, (R)w, f, df);
+    const R g = de * f + e * df;
+    const R ir = (R)1 / r;
+    const double fx = (double)(g * (R)d.x * ir), fy = (double)(g * (R)d.y * ir), fz = (double)(g * (R)d.z * ir);
+    const double h = 0.5 * (double)(e * f);
     if (ca) {
         fpair[3 * (size_t)p] += fx; fpair[3 * (size_t)p + 1] += fy; fpair[3 * (size_t)p + 2] += fz;
         epair[p] += h;
@@ -116,21 +124,41 @@ __global__ void k_gather(int n, const int* __restrict__ Z, const int* __restrict
     for (int k = 0; k < 9; ++k) LV[9 * (size_t)a + k] = escale * v[k];
 }
 
-// Deterministic single-block sums: E = sum le, virial = sum LV.
-__global__ void k_reduce(int n, const double* __restrict__ le, const double* __restrict__ LV, double* __restrict__ out) {
-    __shared__ double sh[10][256];
-    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int a = threadIdx.x; a < n; a += blockDim.x) {
-        acc[0] += le[a];
-        for (int k = 0; k < 9; ++k) acc[1 + k] += LV[9 * (size_t)a + k];
-    }
+// Deterministic sums E = sum le, virial = sum LV in two fixed-order levels: block b
+// reduces atoms [b*RED_CHUNK, (b+1)*RED_CHUNK) into part[b][10]; one block then sums the
+// partials in block order.  No atomics, so the result is bit-identical run to run.
+constexpr int RED_THREADS = 256, RED_CHUNK = 4096;
+
+__device__ __forceinline__ void block_sum10(double (&acc)[10], double (*sh)[RED_THREADS]) {
     for (int k = 0; k < 10; ++k) sh[k][threadIdx.x] = acc[k];
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    for (int s = RED_THREADS / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s)
             for (int k = 0; k < 10; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
         __syncthreads();
     }
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_part(int n, const double* __restrict__ le,
+                                                             const double* __restrict__ LV, double* __restrict__ part) {
+    __shared__ double sh[10][RED_THREADS];
+    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int a0 = blockIdx.x * RED_CHUNK, a1 = min(n, a0 + RED_CHUNK);
+    for (int a = a0 + threadIdx.x; a < a1; a += RED_THREADS) {
+        acc[0] += le[a];
+        for (int k = 0; k < 9; ++k) acc[1 + k] += LV[9 * (size_t)a + k];
+    }
+    block_sum10(acc, sh);
+    if (threadIdx.x < 10) part[10 * blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_final(int nparts, const double* __restrict__ part,
+                                                              double* __restrict__ out) {
+    __shared__ double sh[10][RED_THREADS];
+    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int b = threadIdx.x; b < nparts; b += RED_THREADS)
+        for (int k = 0; k < 10; ++k) acc[k] += part[10 * b + k];
+    block_sum10(acc, sh);
     if (threadIdx.x < 10) out[threadIdx.x] = sh[threadIdx.x][0];
 }
 
@@ -151,7 +179,7 @@ int pair_2b(gapgpu_context& c, const Coordinate& co, int n, const int* d_mask) {
     else
         k_pair_2b<float><<<nb, TB, 0, c.stream>>>(P, c.Z.as<int>(), d_mask, c.nbr_i.as<int>(), c.nbr_j.as<int>(),
                                                   c.nbr_s.as<int>(), c.nbr_rev.as<int>(), c.nbr_d.as<double4>(), co.d2_rc,
-                                                  co.d2_w, co.d2_Z1, co.d2_Z2, co.M, co.dX64, co.dcoef, co.theta[0],
+                                                  co.d2_w, co.d2_Z1, co.d2_Z2, co.M, co.dXf32, co.dcoef32, co.theta[0],
                                                   c.fpair.as<double>(), c.epair.as<double>());
     c.launches++;
     GG_CUDA(cudaGetLastError());
@@ -170,8 +198,12 @@ int gather_outputs(gapgpu_context& c, const gapgpu_model& m, int n, const int* d
                                                     c.nbr_d.as<double4>(), c.fpair.as<double>(), c.epair.as<double>(),
                                                     c.eatom.as<double>(), e0, m.E_scale, c.out_le.as<double>(),
                                                     c.out_f.as<double>(), c.out_lv.as<double>());
-    k_reduce<<<1, 256, 0, c.stream>>>(n, c.out_le.as<double>(), c.out_lv.as<double>(), c.out_e.as<double>());
-    c.launches += 2;
+    const int nparts = (n + RED_CHUNK - 1) / RED_CHUNK;
+    if ((rc = c.redpart.ensure(sizeof(double) * 10 * (size_t)nparts))) return rc;
+    k_reduce_part<<<nparts, RED_THREADS, 0, c.stream>>>(n, c.out_le.as<double>(), c.out_lv.as<double>(),
+                                                       c.redpart.as<double>());
+    k_reduce_final<<<1, RED_THREADS, 0, c.stream>>>(nparts, c.redpart.as<double>(), c.out_e.as<double>());
+    c.launches += 3;
     GG_CUDA(cudaGetLastError());
     return GAPGPU_OK;
 }

@@ -23,16 +23,37 @@
 // neighbour entry n = j; the centre entry is minus the sum over neighbours.
 #include <cub/cub.cuh>
 #include <cmath>
+#include <vector>
 #include "context.h"
 
 namespace gapgpu {
 
-__constant__ double c_ylm_norm[(MAX_LMAX + 1) * (MAX_LMAX + 1)];  // N_lm (sqrt2 folded in for m>0)
-
 namespace {
 
+// Constant block of one SOAP coordinate in the working precision R, uploaded once per
+// model and copied into shared memory by every block (offsets in elements of R):
+//   T[a][n] orthonormalising transform, rb[a] radial grid, cr[n] central-atom l = 0
+//   term, lf[l] = 1/sqrt(2l+1), yn[l*l+m] Ylm normalisation (sqrt2 folded in for m > 0),
+//   ra/rbb[l*l+m] Legendre recurrence P_lm = ra t P_(l-1)m - rbb P_(l-2)m (l >= m+2).
+struct SoapTab {
+    int T, rb, cr, lf, yn, ra, rbb, size;
+};
+__host__ __device__ __forceinline__ SoapTab soap_tab(int nm, int L) {
+    SoapTab t;
+    int o = 0;
+    t.T = o; o += nm * nm;
+    t.rb = o; o += nm;
+    t.cr = o; o += nm;
+    t.lf = o; o += L;
+    t.yn = o; o += L * L;
+    t.ra = o; o += L * L;
+    t.rbb = o; o += L * L;
+    t.size = (o + 7) & ~7;  // keeps what follows 32-byte aligned for R = double
+    return t;
+}
+
 template <class R>
-struct Dual {  // value and gradient with respect to the neighbour's displacement
+struct alignas(4 * sizeof(R)) Dual {  // value and gradient with respect to the neighbour's displacement
     R v, x, y, z;
 };
 template <class R> __device__ __forceinline__ Dual<R> dmul(const Dual<R>& a, const Dual<R>& b) {
@@ -52,6 +73,8 @@ __device__ __forceinline__ double rcos(double x) { return cos(x); }
 __device__ __forceinline__ float rcos(float x) { return cosf(x); }
 __device__ __forceinline__ double rsin(double x) { return sin(x); }
 __device__ __forceinline__ float rsin(float x) { return sinf(x); }
+__device__ __forceinline__ double rinv(double x) { return 1.0 / x; }
+__device__ __forceinline__ float rinv(float x) { return __frcp_rn(x); }
 
 // coordination_function and its derivative
 template <class R>
@@ -67,10 +90,10 @@ __device__ __forceinline__ void cutoff_fn(R r, R rc, R w, R& f, R& df) {
     f = 1; df = 0;
 }
 
-// Column m of the real spherical harmonics Y_lm(d/|d|), l = m..l_max, written to
-// Y[l*l + l +- m].  t = z/r; (cm + i sm) = ((x + i y)/r)^m.
+// Column m of the real spherical harmonics Y_lm(u), l = m..L-1, written to
+// Y[l*l + l +- m] for the unit vector u; (cm + i sm) = (ux + i uy)^m.
 template <class R>
-__device__ void ylm_column(int m, int L, R xr, R yr, R t, R* Y) {
+__device__ void ylm_column(int m, int L, R xr, R yr, R t, const R* __restrict__ K, const SoapTab& tb, R* Y) {
     R cm = 1, sm = 0;
     for (int k = 0; k < m; ++k) {
         R c2 = cm * xr - sm * yr;
@@ -79,16 +102,16 @@ __device__ void ylm_column(int m, int L, R xr, R yr, R t, R* Y) {
     }
     R qmm = 1;
     for (int k = 1; k <= 2 * m - 1; k += 2) qmm *= (R)k;
-    R q2 = qmm, q1 = 0;
+    R q2 = 0, q1 = 0;
     for (int l = m; l < L; ++l) {
+        const int i = l * l + m;
         R q;
         if (l == m) q = qmm;
         else if (l == m + 1) q = (R)(2 * m + 1) * t * qmm;
-        else q = ((R)(2 * l - 1) * t * q1 - (R)(l + m - 1) * q2) / (R)(l - m);
-        if (l > m) q2 = q1;
+        else q = K[tb.ra + i] * t * q1 - K[tb.rbb + i] * q2;
+        q2 = q1;
         q1 = q;
-        if (l == m) q2 = 0;
-        R nrm = (R)c_ylm_norm[l * l + m];
+        const R nrm = K[tb.yn + i];
         if (m == 0) Y[l * l + l] = nrm * q;
         else {
             Y[l * l + l + m] = nrm * q * cm;
@@ -97,15 +120,14 @@ __device__ void ylm_column(int m, int L, R xr, R yr, R t, R* Y) {
     }
 }
 
-// Same column with gradients (dual arithmetic on x, y, z).
+// Same column with gradients (dual arithmetic on the neighbour's x, y, z), from the
+// unit vector u and 1/r: d u_a / d x_b = (delta_ab - u_a u_b) / r.
 template <class R>
-__device__ void ylm_column_grad(int m, int L, R dx, R dy, R dz, R r, Dual<R>* Y) {
-    R ir = (R)1 / r;
-    // xr = x/r etc. with d(x/r)/dx_k = (delta_xk - x x_k / r^2)/r
-    R xr = dx * ir, yr = dy * ir, zr = dz * ir;
-    Dual<R> X = {xr, (1 - xr * xr) * ir, -xr * yr * ir, -xr * zr * ir};
-    Dual<R> Yv = {yr, -yr * xr * ir, (1 - yr * yr) * ir, -yr * zr * ir};
-    Dual<R> T = {zr, -zr * xr * ir, -zr * yr * ir, (1 - zr * zr) * ir};
+__device__ void ylm_column_grad(int m, int L, R xr, R yr, R zr, R ir, const R* __restrict__ K, const SoapTab& tb,
+                                Dual<R>* Y) {
+    const Dual<R> X = {xr, (1 - xr * xr) * ir, -xr * yr * ir, -xr * zr * ir};
+    const Dual<R> Yv = {yr, -yr * xr * ir, (1 - yr * yr) * ir, -yr * zr * ir};
+    const Dual<R> T = {zr, -zr * xr * ir, -zr * yr * ir, (1 - zr * zr) * ir};
     Dual<R> cm = {1, 0, 0, 0}, sm = {0, 0, 0, 0};
     for (int k = 0; k < m; ++k) {
         Dual<R> c2 = dsub(dmul(cm, X), dmul(sm, Yv));
@@ -116,13 +138,14 @@ __device__ void ylm_column_grad(int m, int L, R dx, R dy, R dz, R r, Dual<R>* Y)
     for (int k = 1; k <= 2 * m - 1; k += 2) qmm *= (R)k;
     Dual<R> q1 = {0, 0, 0, 0}, q2 = {0, 0, 0, 0};
     for (int l = m; l < L; ++l) {
+        const int i = l * l + m;
         Dual<R> q;
         if (l == m) q = {qmm, 0, 0, 0};
         else if (l == m + 1) q = dscale((R)(2 * m + 1) * qmm, T);
-        else q = dscale((R)1 / (R)(l - m), dsub(dscale((R)(2 * l - 1), dmul(T, q1)), dscale((R)(l + m - 1), q2)));
-        q2 = (l == m) ? Dual<R>{0, 0, 0, 0} : q1;
+        else q = dsub(dscale(K[tb.ra + i], dmul(T, q1)), dscale(K[tb.rbb + i], q2));
+        q2 = q1;
         q1 = q;
-        R nrm = (R)c_ylm_norm[l * l + m];
+        const R nrm = K[tb.yn + i];
         if (m == 0) Y[l * l + l] = dscale(nrm, q);
         else {
             Y[l * l + l + m] = dscale(nrm, dmul(q, cm));
@@ -131,33 +154,46 @@ __device__ void ylm_column_grad(int m, int L, R dx, R dy, R dz, R r, Dual<R>* Y)
     }
 }
 
-// rho_l(r, r_b) for l = 0..L-1 and (optionally) d/dr.
+// scale * rho_l(r, r_b) -> out[l * stride] for l = 0..L-1 and (when dout is given)
+// d rho_l / dr -> dout[l * stride], with the upward recurrence carried in registers.
 template <class R>
-__device__ void radial_collocation(R r, R rb, R alpha, int L, R* out, R* dout) {
+__device__ void radial_collocation(R r, R rb, R alpha, int L, R scale, R* out, R* dout, int stride) {
     if (rb == (R)0) {
-        R e = rexp(-alpha * r * r);
-        out[0] = e;
+        const R e = rexp(-alpha * r * r);
+        out[0] = scale * e;
         if (dout) dout[0] = -(R)2 * alpha * r * e;
-        for (int l = 1; l < L; ++l) { out[l] = 0; if (dout) dout[l] = 0; }
+        for (int l = 1; l < L; ++l) { out[l * stride] = 0; if (dout) dout[l * stride] = 0; }
         return;
     }
-    R x = (R)2 * alpha * r * rb;
-    R em = rexp(-alpha * (r - rb) * (r - rb));
-    R ep = rexp(-alpha * (r + rb) * (r + rb));
-    R ix = (R)1 / x;
-    out[0] = (R)0.5 * (em - ep) * ix;
-    if (L > 1) out[1] = (R)0.5 * (em + ep) * ix - (R)0.5 * (em - ep) * ix * ix;
-    for (int l = 2; l < L; ++l) out[l] = out[l - 2] - (R)(2 * l - 1) * out[l - 1] * ix;
-    if (dout) {
-        // d/dr with dx/dr = 2 alpha rb, dem/dr = -2 alpha (r - rb) em, dep/dr = -2 alpha (r + rb) ep
-        R dx = (R)2 * alpha * rb;
-        R dem = -(R)2 * alpha * (r - rb) * em, dep = -(R)2 * alpha * (r + rb) * ep;
-        R dix = -dx * ix * ix;
-        dout[0] = (R)0.5 * (dem - dep) * ix + (R)0.5 * (em - ep) * dix;
-        if (L > 1)
-            dout[1] = (R)0.5 * (dem + dep) * ix + (R)0.5 * (em + ep) * dix - (R)0.5 * (dem - dep) * ix * ix -
-                      (R)0.5 * (em - ep) * (R)2 * ix * dix;
-        for (int l = 2; l < L; ++l) dout[l] = dout[l - 2] - (R)(2 * l - 1) * (dout[l - 1] * ix + out[l - 1] * dix);
+    const R x = (R)2 * alpha * r * rb;
+    const R em = rexp(-alpha * (r - rb) * (r - rb));
+    const R ep = rexp(-alpha * (r + rb) * (r + rb));
+    const R ix = rinv(x);
+    // d/dr with dx/dr = 2 alpha rb, dem/dr = -2 alpha (r - rb) em, dep/dr = -2 alpha (r + rb) ep
+    const R dx = (R)2 * alpha * rb;
+    const R dem = -(R)2 * alpha * (r - rb) * em, dep = -(R)2 * alpha * (r + rb) * ep;
+    const R dix = -dx * ix * ix;
+    R v0 = (R)0.5 * (em - ep) * ix;
+    R d0 = (R)0.5 * (dem - dep) * ix + (R)0.5 * (em - ep) * dix;
+    out[0] = scale * v0;
+    if (dout) dout[0] = d0;
+    if (L < 2) return;
+    R v1 = (R)0.5 * (em + ep) * ix - (R)0.5 * (em - ep) * ix * ix;
+    R d1 = (R)0.5 * (dem + dep) * ix + (R)0.5 * (em + ep) * dix - (R)0.5 * (dem - dep) * ix * ix -
+           (R)0.5 * (em - ep) * (R)2 * ix * dix;
+    out[stride] = scale * v1;
+    if (dout) dout[stride] = d1;
+    for (int l = 2; l < L; ++l) {
+        const R v2 = v0 - (R)(2 * l - 1) * v1 * ix;
+        out[l * stride] = scale * v2;
+        if (dout) {
+            const R d2 = d0 - (R)(2 * l - 1) * (d1 * ix + v1 * dix);
+            dout[l * stride] = d2;
+            d0 = d1;
+            d1 = d2;
+        }
+        v0 = v1;
+        v1 = v2;
     }
 }
 
@@ -167,102 +203,156 @@ __device__ __forceinline__ int species_channel(const SoapConst& sc, int z) {
     return -1;
 }
 
+// Row pr of the power spectrum -> (ia, jb <= ia), pr = ia (ia + 1) / 2 + jb.  The FP32
+// square root is a first guess (exact for pr < 2^21); the loops make the result exact.
 __device__ __forceinline__ void decode_pair(int pr, int& ia, int& jb) {
-    int a = (int)((sqrt(8.0 * pr + 1.0) - 1.0) * 0.5);
+    int a = (int)((sqrtf((float)(8 * pr + 1)) - 1.0f) * 0.5f);
     while ((a + 1) * (a + 2) / 2 <= pr) ++a;
     while (a * (a + 1) / 2 > pr) --a;
     ia = a;
     jb = pr - a * (a + 1) / 2;
 }
 
-constexpr int FWD_THREADS = 128;
-constexpr int TC = 32;  // neighbours staged per chunk (one warp builds the species lists)
+__device__ __forceinline__ int l_of_lm(int lm) {
+    int l = (int)sqrtf((float)lm);
+    while ((l + 1) * (l + 1) <= lm) ++l;
+    while (l * l > lm) --l;
+    return l;
+}
 
-__constant__ unsigned char c_l_of_lm[(MAX_LMAX + 1) * (MAX_LMAX + 1)];
+constexpr int FWD_THREADS = 128;
+constexpr int TC = 32;   // neighbours staged per chunk in the forward kernel
+constexpr int TCB = 16;  // ... and in the backward kernel (dual Ylm staging is 4x larger)
 
 __host__ __device__ __forceinline__ int nmp_of(int nm) { return (nm + 3) & ~3; }
 
 // Per-chunk set-up by warp 0: species channel of each staged neighbour and, per
 // species, the list of staged neighbours in staging order (deterministic).
+template <int TCX>
 __device__ __forceinline__ void build_species_lists(const SoapConst& sc, int base, int cnt, const int* __restrict__ Z,
                                                     const int* __restrict__ nj, const double4* __restrict__ nd, int* spc,
                                                     int* lst, int* lcnt) {
     const int lane = threadIdx.x & 31;
     int s = -1;
     if (lane < cnt) {
-        double4 d = nd[base + lane];
-        s = (d.w < sc.rc) ? species_channel(sc, Z[nj[base + lane]]) : -1;
-        spc[lane] = s;
+        const double r = nd[base + lane].w;
+        s = (r < sc.rc) ? species_channel(sc, Z[nj[base + lane]]) : -1;
     }
+    if (lane < TCX) spc[lane] = s;
     const unsigned lt = (1u << lane) - 1u;
     for (int k = 0; k < sc.n_species; ++k) {
         unsigned m = __ballot_sync(0xffffffffu, s == k);
-        if (s == k) lst[k * TC + __popc(m & lt)] = lane;
+        if (s == k) lst[k * TCX + __popc(m & lt)] = lane;
         if (lane == 0) lcnt[k] = __popc(m);
     }
 }
 
+// Stage neighbour t of the chunk: unit vector, 1/r and r in R (one conversion from the
+// FP64 list per neighbour), cutoff function and its derivative.
+template <class R>
+__device__ __forceinline__ void stage_neighbour(const SoapConst& sc, const double4& d, R* dsm, R* fcs, R* dfcs) {
+    const R r = (R)d.w, ir = rinv(r);
+    dsm[0] = (R)d.x * ir;
+    dsm[1] = (R)d.y * ir;
+    dsm[2] = (R)d.z * ir;
+    dsm[3] = ir;
+    dsm[4] = r;
+    R f, df;
+    cutoff_fn<R>(r, (R)sc.rc, (R)sc.w, f, df);
+    *fcs = f;
+    if (dfcs) *dfcs = df;
+}
+constexpr int DS = 5;  // staged values per neighbour: ux, uy, uz, 1/r, r
+
+// sum_e h[e] * x[e] over NMP entries (NMP a multiple of 4), two right-hand sides.
+__device__ __forceinline__ void dot2(const float* __restrict__ h, const float* __restrict__ x, const float* __restrict__ y,
+                                     int NMP, float& u, float& w) {
+    const float4* h4 = reinterpret_cast<const float4*>(h);
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    const float4* y4 = reinterpret_cast<const float4*>(y);
+    for (int a = 0; a < NMP / 4; ++a) {
+        const float4 hh = h4[a], xx = x4[a], yy = y4[a];
+        u += hh.x * xx.x + hh.y * xx.y + hh.z * xx.z + hh.w * xx.w;
+        w += hh.x * yy.x + hh.y * yy.y + hh.z * yy.z + hh.w * yy.w;
+    }
+}
+__device__ __forceinline__ void dot2(const double* __restrict__ h, const double* __restrict__ x,
+                                     const double* __restrict__ y, int NMP, double& u, double& w) {
+    for (int a = 0; a < NMP; ++a) {
+        u += h[a] * x[a];
+        w += h[a] * y[a];
+    }
+}
+
+template <class R>
+__device__ __forceinline__ void load_tab(const R* __restrict__ tab, R* K, int n) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) K[k] = tab[k];
+}
+
 // Forward: one block per centre.  Densities are accumulated in the collocation basis
 // ct[s][lm][a] = sum_j fc rho_l(r_j, r_a) Y_lm(r^_j); the orthonormalising transform
-// c[s][n][lm] = sum_a T_an ct[s][lm][a] is applied once per centre.
+// c[s][n][lm] = sum_a T_an ct[s][lm][a] is applied once per centre.  In the mixed path
+// everything is FP32 except the norm reduction (per-thread FP32 partial sums combined
+// in FP64) and 1/|p|.
 template <class R>
-__global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int nc, const int* __restrict__ centres,
-                                                               const int* __restrict__ Z, const int* __restrict__ off,
-                                                               const int* __restrict__ nj, const double4* __restrict__ nd,
-                                                               R* __restrict__ c_out, R* __restrict__ q_out,
-                                                               double* __restrict__ pnorm) {
+__global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, const R* __restrict__ tab, int nc,
+                                                               const int* __restrict__ centres, const int* __restrict__ Z,
+                                                               const int* __restrict__ off, const int* __restrict__ nj,
+                                                               const double4* __restrict__ nd, R* __restrict__ c_out,
+                                                               R* __restrict__ q_out, double* __restrict__ pnorm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ci = blockIdx.x;
     if (ci >= nc) return;
     const int atom = centres[ci];
     const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, NMP = nmp_of(nm), NS = sc.n_species;
-    R* ct = reinterpret_cast<R*>(smem_raw);          // NS * L2 * NMP
+    const SoapTab tb = soap_tab(nm, L);
+    R* K = reinterpret_cast<R*>(smem_raw);           // tb.size
+    R* ct = K + tb.size;                              // NS * L2 * NMP
     R* cs = ct + NS * L2 * NMP;                       // NS * nm * L2
-    R* Ysm = cs + NS * nm * L2;                       // TC * L2
+    R* Ysm = cs + NS * nm * L2;                       // TC * L2          (power spectrum reuses this region)
     R* Ism = Ysm + TC * L2;                           // TC * L * NMP
     R* fcs = Ism + TC * L * NMP;                      // TC
-    int* spc = reinterpret_cast<int*>(fcs + TC);      // TC
+    R* dsm = fcs + TC;                                // TC * DS
+    const int stage = TC * L2 + TC * L * NMP + TC + TC * DS, ps_len = sc.n_pairs * L;
+    int* spc = reinterpret_cast<int*>(Ysm + (stage > ps_len ? stage : ps_len));  // TC
     int* lst = spc + TC;                              // NS * TC
     int* lcnt = lst + NS * TC;                        // NS
     const int tid = threadIdx.x;
+    load_tab(tab, K, tb.size);
     for (int k = tid; k < NS * L2 * NMP; k += blockDim.x) ct[k] = 0;
+    const R alpha = (R)sc.alpha;
     const int p0 = off[atom], p1 = off[atom + 1];
     for (int base = p0; base < p1; base += TC) {
         const int cnt = min(TC, p1 - base);
         __syncthreads();
-        if (tid < 32) build_species_lists(sc, base, cnt, Z, nj, nd, spc, lst, lcnt);
-        if (tid < cnt) {
-            R f, df;
-            cutoff_fn<R>((R)nd[base + tid].w, (R)sc.rc, (R)sc.w, f, df);
-            fcs[tid] = f;
+        if (tid < 32) build_species_lists<TC>(sc, base, cnt, Z, nj, nd, spc, lst, lcnt);
+        else if (tid - 32 < cnt) {
+            const int t = tid - 32;
+            stage_neighbour<R>(sc, nd[base + t], dsm + DS * t, fcs + t, (R*)nullptr);
         }
         __syncthreads();
         for (int k = tid; k < cnt * L; k += blockDim.x) {
-            int t = k / L, m = k % L;
+            const int t = k / L, m = k % L;
             if (spc[t] < 0) continue;
-            double4 d = nd[base + t];
-            R ir = (R)1 / (R)d.w;
-            ylm_column<R>(m, L, (R)d.x * ir, (R)d.y * ir, (R)d.z * ir, Ysm + t * L2);
+            const R* u = dsm + DS * t;
+            ylm_column<R>(m, L, u[0], u[1], u[2], K, tb, Ysm + t * L2);
         }
         for (int k = tid; k < cnt * NMP; k += blockDim.x) {
-            int t = k / NMP, a = k % NMP;
+            const int t = k / NMP, a = k % NMP;
             if (spc[t] < 0) continue;
             R* out = Ism + t * L * NMP + a;
             if (a >= nm) {
                 for (int l = 0; l < L; ++l) out[l * NMP] = 0;
                 continue;
             }
-            R rho[MAX_LMAX + 1];
-            radial_collocation<R>((R)nd[base + t].w, (R)sc.rb[a], (R)sc.alpha, L, rho, nullptr);
-            const R f = fcs[t];
-            for (int l = 0; l < L; ++l) out[l * NMP] = f * rho[l];
+            radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, fcs[t], out, (R*)nullptr, NMP);
         }
         __syncthreads();
         // ct[s][lm][a..a+3] += sum_{t in species s} Y[t][lm] I[t][l][a..a+3]
         const int NA4 = NMP / 4;
         for (int k = tid; k < NS * L2 * NA4; k += blockDim.x) {
             const int s = k / (L2 * NA4), rem = k % (L2 * NA4), lm = rem / NA4, a4 = rem % NA4;
-            const int l = c_l_of_lm[lm];
+            const int l = l_of_lm(lm);
             R a0 = 0, a1 = 0, a2 = 0, a3 = 0;
             const int nt = lcnt[s];
             const int* ls = lst + s * TC;
@@ -283,8 +373,8 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int 
         const int s = k / (nm * L2), rem = k % (nm * L2), n = rem / L2, lm = rem % L2;
         const R* v = ct + (s * L2 + lm) * NMP;
         R acc = 0;
-        for (int a = 0; a < nm; ++a) acc += (R)sc.T[a * nm + n] * v[a];
-        if (lm == 0 && (sc.centre_all || sc.species_Z[s] == zc || sc.species_Z[s] == 0)) acc += (R)sc.centre_R[n];
+        for (int a = 0; a < nm; ++a) acc += K[tb.T + a * nm + n] * v[a];
+        if (lm == 0 && (sc.centre_all || sc.species_Z[s] == zc || sc.species_Z[s] == 0)) acc += K[tb.cr + n];
         cs[k] = acc;
     }
     __syncthreads();
@@ -292,7 +382,7 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int 
     for (int k = tid; k < sc.ncomp; k += blockDim.x) cg[k] = cs[k];
     // power spectrum: one item per (ia, jb) pair, all l
     R* ps = Ysm;
-    double ss = 0;
+    R ssr = 0;
     for (int pr = tid; pr < sc.n_pairs; pr += blockDim.x) {
         int ia, jb;
         decode_pair(pr, ia, jb);
@@ -302,26 +392,27 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int 
         for (int l = 0; l < L; ++l) {
             R v = 0;
             for (int m = l * l; m < (l + 1) * (l + 1); ++m) v += ca[m] * cb[m];
-            v *= off2 * rsqrt((R)(2 * l + 1));
+            v *= off2 * K[tb.lf + l];
             ps[pr * L + l] = v;
-            ss += (double)v * (double)v;
+            ssr += v * v;
         }
     }
     typedef cub::BlockReduce<double, FWD_THREADS> BR;
     __shared__ typename BR::TempStorage tmps;
-    double tot = BR(tmps).Sum(ss);
-    __shared__ double s_norm;
+    const double tot = BR(tmps).Sum((double)ssr);
+    __shared__ double s_inv;
     if (tid == 0) {
-        s_norm = sqrt(tot);
-        pnorm[ci] = s_norm;
+        const double nrm = sqrt(tot);
+        pnorm[ci] = nrm;
+        s_inv = sc.normalise ? 1.0 / nrm : 1.0;
     }
     __syncthreads();
-    const double inv = sc.normalise ? 1.0 / s_norm : 1.0;
+    const R inv = (R)s_inv;
     const int np = sc.n_pairs * L;
     R* qg = q_out + (size_t)ci * sc.dpad;
     for (int k = tid; k < sc.dpad; k += blockDim.x) {
         R v;
-        if (k < np) v = (R)((double)ps[k] * inv);
+        if (k < np) v = ps[k] * inv;
         else if (k == np) v = (R)sc.sigma0;
         else v = 0;
         qg[k] = v;
@@ -331,68 +422,99 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, int 
 constexpr int BWD_THREADS = 128;
 constexpr int BWD_WARPS = BWD_THREADS / 32;
 
+// Shared-memory plan of the backward kernel (elements of R): constant block, h, then a
+// region used first for (c, dE/dc, dE/dp) and then for the neighbour staging.
+struct BwdPlan {
+    int hs, U, pre, stage, ints_at;
+};
+__host__ __device__ __forceinline__ BwdPlan bwd_plan(const SoapConst& sc) {
+    const int L = sc.l_max + 1, L2 = L * L, NMP = nmp_of(sc.n_max), NS = sc.n_species;
+    BwdPlan p;
+    p.hs = soap_tab(sc.n_max, L).size;
+    p.U = p.hs + ((NS * L2 * NMP + 7) & ~7);
+    p.pre = 2 * sc.ncomp + sc.n_pairs * L;
+    p.stage = 4 * TCB * L2 + 2 * TCB * L * NMP + (2 + DS) * TCB;
+    p.ints_at = p.U + (((p.pre > p.stage ? p.pre : p.stage) + 7) & ~7);
+    return p;
+}
+
 // Backward: one block per centre.
-//   dE/dp (FP64 normalisation Jacobian) -> H_l[a][b]
+//   dE/dp (normalisation Jacobian: FP64 scalars q.G and 1/|p|) -> H_l[a][b]
 //   dE/dc[a][lm] = sum_b H_l[a][b] c[b][lm]
 //   h[s][lm][a'] = sum_n T_a'n dE/dc[s][n][lm]        (back to the collocation basis)
 //   per pair t of species s:  u_lm = sum_a h[s][lm][a] rho_al(r),  w_lm = sum_a h[s][lm][a] drho_al/dr
 //   f_t = sum_lm [(fc w_lm + fc' u_lm) Y_lm r^ + fc u_lm grad Y_lm]
 template <class R>
-__global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, int nc, const int* __restrict__ centres,
-                                                                const int* __restrict__ Z, const int* __restrict__ off,
-                                                                const int* __restrict__ nj, const double4* __restrict__ nd,
-                                                                const R* __restrict__ c_in, const R* __restrict__ q_in,
-                                                                const double* __restrict__ pnorm, const R* __restrict__ G,
-                                                                double* __restrict__ fpair) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, const R* __restrict__ tab, int nc,
+                                                                const int* __restrict__ centres, const int* __restrict__ Z,
+                                                                const int* __restrict__ off, const int* __restrict__ nj,
+                                                                const double4* __restrict__ nd, const R* __restrict__ c_in,
+                                                                const R* __restrict__ q_in, const double* __restrict__ pnorm,
+                                                                const R* __restrict__ G, double* __restrict__ fpair) {
+    extern __shared__ __align__(32) unsigned char smem_raw[];
     const int ci = blockIdx.x;
     if (ci >= nc) return;
     const int atom = centres[ci];
     const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, NMP = nmp_of(nm), NS = sc.n_species, NN = NS * nm;
     const int np = sc.n_pairs * L;
-    R* hs = reinterpret_cast<R*>(smem_raw);            // NS * L2 * NMP
-    R* cs = hs + NS * L2 * NMP;                         // ncomp (c, then dE/dc in place of a copy)
+    const SoapTab tb = soap_tab(nm, L);
+    const BwdPlan pl = bwd_plan(sc);
+    R* K = reinterpret_cast<R*>(smem_raw);
+    R* hs = K + pl.hs;                                  // NS * L2 * NMP
+    R* U = K + pl.U;
+    // pre-phase view of U
+    R* cs = U;                                          // ncomp
     R* dc = cs + sc.ncomp;                              // ncomp
-    R* dp = dc + sc.ncomp;                              // np (H values)
-    Dual<R>* Yd = reinterpret_cast<Dual<R>*>(dp + np);  // TC * L2
-    R* Ism = reinterpret_cast<R*>(Yd + TC * L2);        // TC * L * NMP
-    R* dIsm = Ism + TC * L * NMP;                       // TC * L * NMP
-    R* fcs = dIsm + TC * L * NMP;                       // TC
-    R* dfcs = fcs + TC;                                 // TC
-    int* spc = reinterpret_cast<int*>(dfcs + TC);       // TC
-    int* lst = spc + TC;                                // NS * TC (unused order; kept for the shared set-up)
-    int* lcnt = lst + NS * TC;                          // NS
+    R* dp = dc + sc.ncomp;                              // np
+    // staging view of U
+    Dual<R>* Yd = reinterpret_cast<Dual<R>*>(U);        // TCB * L2
+    R* Ism = U + 4 * TCB * L2;                          // TCB * L * NMP
+    R* dIsm = Ism + TCB * L * NMP;                      // TCB * L * NMP
+    R* fcs = dIsm + TCB * L * NMP;                      // TCB
+    R* dfcs = fcs + TCB;                                // TCB
+    R* dsm = dfcs + TCB;                                // TCB * DS
+    int* spc = reinterpret_cast<int*>(K + pl.ints_at);  // TCB
+    int* lst = spc + TCB;                               // NS * TCB
+    int* lcnt = lst + NS * TCB;                         // NS
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    load_tab(tab, K, tb.size);
     const R* cg = c_in + (size_t)ci * sc.ncomp;
     for (int k = tid; k < sc.ncomp; k += blockDim.x) cs[k] = cg[k];
     const R* qg = q_in + (size_t)ci * sc.dpad;
     const R* gg = G + (size_t)ci * sc.dpad;
-    double qd = 0;
-    for (int k = tid; k < np; k += blockDim.x) qd += (double)qg[k] * (double)gg[k];
+    R part = 0;
+    for (int k = tid; k < np; k += blockDim.x) part += qg[k] * gg[k];
     typedef cub::BlockReduce<double, BWD_THREADS> BR;
     __shared__ typename BR::TempStorage tmps;
-    double tot = BR(tmps).Sum(qd);
-    __shared__ double s_qg;
-    if (tid == 0) s_qg = tot;
+    const double tot = BR(tmps).Sum((double)part);
+    __shared__ double s_qg, s_inv;
+    if (tid == 0) {
+        s_qg = tot;
+        s_inv = 1.0 / pnorm[ci];
+    }
     __syncthreads();
-    const double nrm = pnorm[ci];
-    for (int k = tid; k < np; k += blockDim.x) {
-        double v = sc.normalise ? ((double)gg[k] - (double)qg[k] * s_qg) / nrm : (double)gg[k];
-        int l = k % L;
-        int pr = k / L, ia, jb;
+    const R sq = (R)s_qg, inv = (R)s_inv;
+    for (int pr = tid; pr < sc.n_pairs; pr += blockDim.x) {
+        int ia, jb;
         decode_pair(pr, ia, jb);
-        double fac = (ia != jb ? 1.41421356237309504880 : 2.0) / sqrt((double)(2 * l + 1));
-        dp[k] = (R)(v * fac);
+        const R f0 = ia != jb ? (R)1.41421356237309504880 : (R)2;
+        for (int l = 0; l < L; ++l) {
+            const int k = pr * L + l;
+            const R v = sc.normalise ? (gg[k] - qg[k] * sq) * inv : gg[k];
+            dp[k] = v * f0 * K[tb.lf + l];
+        }
     }
     __syncthreads();
     for (int k = tid; k < sc.ncomp; k += blockDim.x) {
-        const int a = k / L2, lm = k % L2;
-        const int l = c_l_of_lm[lm];
+        const int a = k / L2, lm = k - a * L2;
+        const int l = l_of_lm(lm);
         R acc = 0;
-        const int rowa = a * (a + 1) / 2;
-        for (int b = 0; b < NN; ++b) {
-            const int idx = (b <= a ? rowa + b : b * (b + 1) / 2 + a) * L + l;
+        int idx = (a * (a + 1) / 2) * L + l;  // pair (a, b = 0)
+        for (int b = 0; b <= a; ++b, idx += L) acc += dp[idx] * cs[b * L2 + lm];
+        idx = ((a + 1) * (a + 2) / 2 + a) * L + l;  // pair (b = a + 1, a)
+        for (int b = a + 1; b < NN; ++b) {
             acc += dp[idx] * cs[b * L2 + lm];
+            idx += (b + 1) * L;
         }
         dc[k] = acc;
     }
@@ -401,29 +523,28 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, int
         const int s = k / (L2 * NMP), rem = k % (L2 * NMP), lm = rem / NMP, a = rem % NMP;
         R acc = 0;
         if (a < nm)
-            for (int n = 0; n < nm; ++n) acc += (R)sc.T[a * nm + n] * dc[(s * nm + n) * L2 + lm];
+            for (int n = 0; n < nm; ++n) acc += K[tb.T + a * nm + n] * dc[(s * nm + n) * L2 + lm];
         hs[k] = acc;
     }
+    const R alpha = (R)sc.alpha;
     const int p0 = off[atom], p1 = off[atom + 1];
-    for (int base = p0; base < p1; base += TC) {
-        const int cnt = min(TC, p1 - base);
+    for (int base = p0; base < p1; base += TCB) {
+        const int cnt = min(TCB, p1 - base);
         __syncthreads();
-        if (tid < 32) build_species_lists(sc, base, cnt, Z, nj, nd, spc, lst, lcnt);
-        if (tid < cnt) {
-            R f, df;
-            cutoff_fn<R>((R)nd[base + tid].w, (R)sc.rc, (R)sc.w, f, df);
-            fcs[tid] = f;
-            dfcs[tid] = df;
+        if (tid < 32) build_species_lists<TCB>(sc, base, cnt, Z, nj, nd, spc, lst, lcnt);
+        else if (tid - 32 < cnt) {
+            const int t = tid - 32;
+            stage_neighbour<R>(sc, nd[base + t], dsm + DS * t, fcs + t, dfcs + t);
         }
         __syncthreads();
         for (int k = tid; k < cnt * L; k += blockDim.x) {
-            int t = k / L, m = k % L;
+            const int t = k / L, m = k % L;
             if (spc[t] < 0) continue;
-            double4 d = nd[base + t];
-            ylm_column_grad<R>(m, L, (R)d.x, (R)d.y, (R)d.z, (R)d.w, Yd + t * L2);
+            const R* u = dsm + DS * t;
+            ylm_column_grad<R>(m, L, u[0], u[1], u[2], u[3], K, tb, Yd + t * L2);
         }
         for (int k = tid; k < cnt * NMP; k += blockDim.x) {
-            int t = k / NMP, a = k % NMP;
+            const int t = k / NMP, a = k % NMP;
             if (spc[t] < 0) continue;
             R* o = Ism + t * L * NMP + a;
             R* od = dIsm + t * L * NMP + a;
@@ -431,35 +552,22 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, int
                 for (int l = 0; l < L; ++l) { o[l * NMP] = 0; od[l * NMP] = 0; }
                 continue;
             }
-            R rho[MAX_LMAX + 1], drho[MAX_LMAX + 1];
-            radial_collocation<R>((R)nd[base + t].w, (R)sc.rb[a], (R)sc.alpha, L, rho, drho);
-            for (int l = 0; l < L; ++l) { o[l * NMP] = rho[l]; od[l * NMP] = drho[l]; }
+            radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, (R)1, o, od, NMP);
         }
         __syncthreads();
-        const int NA4 = NMP / 4;
         for (int t = wid; t < cnt; t += BWD_WARPS) {
             const int s = spc[t];
             if (s < 0) continue;  // warp-uniform
-            const double4 d = nd[base + t];
-            const R ir = (R)1 / (R)d.w, ux = (R)d.x * ir, uy = (R)d.y * ir, uz = (R)d.z * ir;
+            const R* u = dsm + DS * t;
+            const R ux = u[0], uy = u[1], uz = u[2];
             const R f = fcs[t], df = dfcs[t];
             R fx = 0, fy = 0, fz = 0;
             for (int lm = lane; lm < L2; lm += 32) {
-                const int l = c_l_of_lm[lm];
-                const R* hv = hs + (s * L2 + lm) * NMP;
-                const R* iv = Ism + (t * L + l) * NMP;
-                const R* jv = dIsm + (t * L + l) * NMP;
-                R u = 0, w = 0;
-                for (int a4 = 0; a4 < NA4; ++a4) {
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const R hh = hv[4 * a4 + e];
-                        u += hh * iv[4 * a4 + e];
-                        w += hh * jv[4 * a4 + e];
-                    }
-                }
+                const int l = l_of_lm(lm);
+                R uu = 0, ww = 0;
+                dot2(hs + (s * L2 + lm) * NMP, Ism + (t * L + l) * NMP, dIsm + (t * L + l) * NMP, NMP, uu, ww);
                 const Dual<R> y = Yd[t * L2 + lm];
-                const R rad = (f * w + df * u) * y.v, ang = f * u;
+                const R rad = (f * ww + df * uu) * y.v, ang = f * uu;
                 fx += rad * ux + ang * y.x;
                 fy += rad * uy + ang * y.y;
                 fz += rad * uz + ang * y.z;
@@ -494,43 +602,18 @@ __global__ void k_iota(int n, int* out) {
     if (a < n) out[a] = a;
 }
 
-bool g_norm_ready[64] = {false};
-
-int ensure_ylm_norm() {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 64 && g_norm_ready[dev]) return GAPGPU_OK;
-    double h[(MAX_LMAX + 1) * (MAX_LMAX + 1)] = {0};
-    for (int l = 0; l <= MAX_LMAX; ++l)
-        for (int m = 0; m <= l; ++m) {
-            double lf = 1.0;
-            for (int k = l - m + 1; k <= l + m; ++k) lf /= k;
-            double N = std::sqrt((2 * l + 1) / (4.0 * M_PI) * lf);
-            h[l * l + m] = m == 0 ? N : std::sqrt(2.0) * N;
-        }
-    GG_CUDA(cudaMemcpyToSymbol(c_ylm_norm, h, sizeof h));
-    unsigned char lt[(MAX_LMAX + 1) * (MAX_LMAX + 1)];
-    for (int l = 0; l <= MAX_LMAX; ++l)
-        for (int k = l * l; k < (l + 1) * (l + 1); ++k) lt[k] = (unsigned char)l;
-    GG_CUDA(cudaMemcpyToSymbol(c_l_of_lm, lt, sizeof lt));
-    if (dev < 64) g_norm_ready[dev] = true;
-    return GAPGPU_OK;
-}
-
 template <class R>
 size_t fwd_smem(const SoapConst& sc) {
     const int L = sc.l_max + 1, L2 = L * L, NMP = nmp_of(sc.n_max), NS = sc.n_species;
-    size_t stage = (size_t)TC * L2 + (size_t)TC * L * NMP + TC;
-    size_t ps = (size_t)sc.n_pairs * L;
-    return sizeof(R) * ((size_t)NS * L2 * NMP + (size_t)NS * sc.n_max * L2 + std::max(stage, ps)) +
+    const size_t stage = (size_t)TC * L2 + (size_t)TC * L * NMP + TC + TC * DS;
+    const size_t ps = (size_t)sc.n_pairs * L;
+    return sizeof(R) * ((size_t)soap_tab(sc.n_max, L).size + (size_t)NS * L2 * NMP + (size_t)NS * sc.n_max * L2 +
+                        std::max(stage, ps)) +
            sizeof(int) * (TC + NS * TC + NS) + 64;
 }
 template <class R>
 size_t bwd_smem(const SoapConst& sc) {
-    const int L = sc.l_max + 1, L2 = L * L, NMP = nmp_of(sc.n_max), NS = sc.n_species;
-    return sizeof(R) * ((size_t)NS * L2 * NMP + 2 * (size_t)sc.ncomp + (size_t)sc.n_pairs * L + 4 * (size_t)TC * L2 +
-                        2 * (size_t)TC * L * NMP + 2 * TC) +
-           sizeof(int) * (TC + NS * TC + NS) + 64;
+    return sizeof(R) * (size_t)bwd_plan(sc).ints_at + sizeof(int) * (TCB + sc.n_species * TCB + sc.n_species) + 64;
 }
 
 template <class R>
@@ -539,9 +622,10 @@ int launch_forward(gapgpu_context& c, const Coordinate& co, int nc) {
     size_t sm = fwd_smem<R>(sc);
     if (sm > 200 * 1024) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the shared-memory forward kernel");
     GG_CUDA(cudaFuncSetAttribute(k_soap_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_soap_forward<R><<<nc, FWD_THREADS, sm, c.stream>>>(sc, nc, c.centres.as<int>(), c.Z.as<int>(), c.nbr_off.as<int>(),
-                                                         c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.scratch.as<R>(),
-                                                         c.qbuf.as<R>(), c.pnorm.as<double>());
+    const R* tab = static_cast<const R*>(co.dtab[sizeof(R) == 4 ? 1 : 0]);
+    k_soap_forward<R><<<nc, FWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.centres.as<int>(), c.Z.as<int>(),
+                                                         c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(),
+                                                         c.scratch.as<R>(), c.qbuf.as<R>(), c.pnorm.as<double>());
     c.launches++;
     GG_CUDA(cudaGetLastError());
     return GAPGPU_OK;
@@ -553,10 +637,11 @@ int launch_backward(gapgpu_context& c, const Coordinate& co, int nc) {
     size_t sm = bwd_smem<R>(sc);
     if (sm > 200 * 1024) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the shared-memory backward kernel");
     GG_CUDA(cudaFuncSetAttribute(k_soap_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_soap_backward<R><<<nc, BWD_THREADS, sm, c.stream>>>(sc, nc, c.centres.as<int>(), c.Z.as<int>(), c.nbr_off.as<int>(),
-                                                          c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.scratch.as<R>(),
-                                                          c.qbuf.as<R>(), c.pnorm.as<double>(), c.Gbuf.as<R>(),
-                                                          c.fpair.as<double>());
+    const R* tab = static_cast<const R*>(co.dtab[sizeof(R) == 4 ? 1 : 0]);
+    k_soap_backward<R><<<nc, BWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.centres.as<int>(), c.Z.as<int>(),
+                                                          c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(),
+                                                          c.scratch.as<R>(), c.qbuf.as<R>(), c.pnorm.as<double>(),
+                                                          c.Gbuf.as<R>(), c.fpair.as<double>());
     c.launches++;
     GG_CUDA(cudaGetLastError());
     return GAPGPU_OK;
@@ -564,12 +649,39 @@ int launch_backward(gapgpu_context& c, const Coordinate& co, int nc) {
 
 }  // namespace
 
+int upload_soap_tables(Coordinate& co) {
+    const SoapParams& sp = co.soap;
+    const int nm = sp.n_max, L = sp.l_max + 1;
+    const SoapTab tb = soap_tab(nm, L);
+    std::vector<double> h(tb.size, 0.0);
+    for (int k = 0; k < nm * nm; ++k) h[tb.T + k] = sp.T[k];
+    for (int a = 0; a < nm; ++a) { h[tb.rb + a] = sp.rb[a]; h[tb.cr + a] = sp.centre_R[a]; }
+    for (int l = 0; l < L; ++l) {
+        h[tb.lf + l] = 1.0 / std::sqrt((double)(2 * l + 1));
+        for (int m = 0; m <= l; ++m) {
+            double lf = 1.0;
+            for (int k = l - m + 1; k <= l + m; ++k) lf /= k;
+            const double N = std::sqrt((2 * l + 1) / (4.0 * M_PI) * lf);
+            h[tb.yn + l * l + m] = m == 0 ? N : std::sqrt(2.0) * N;
+            if (l >= m + 2) {
+                h[tb.ra + l * l + m] = (double)(2 * l - 1) / (double)(l - m);
+                h[tb.rbb + l * l + m] = (double)(l + m - 1) / (double)(l - m);
+            }
+        }
+    }
+    std::vector<float> f(h.begin(), h.end());
+    GG_CUDA(cudaMalloc(&co.dtab[0], sizeof(double) * h.size()));
+    GG_CUDA(cudaMalloc(&co.dtab[1], sizeof(float) * f.size()));
+    GG_CUDA(cudaMemcpy(co.dtab[0], h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    GG_CUDA(cudaMemcpy(co.dtab[1], f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+    return GAPGPU_OK;
+}
+
 int select_centres(gapgpu_context& c, const Coordinate& co, int n, const int* d_mask, int* nc_out) {
     int rc;
     if ((rc = c.flags.ensure(sizeof(int) * n)) || (rc = c.centres.ensure(sizeof(int) * n)) ||
         (rc = c.ncent.ensure(sizeof(int) * 2)) || (rc = c.eatom.ensure(sizeof(double) * n)))
         return rc;
-    if ((rc = ensure_ylm_norm())) return rc;
     SoapConst sc = soap_const(co);
     int zl[MAX_CENTRE_Z];
     for (int k = 0; k < co.soap.n_Z; ++k) zl[k] = co.soap.Z[k];

@@ -21,6 +21,7 @@
 #include <cstring>
 #include <cmath>
 #include <vector>
+#include <algorithm>
 
 #include "context.h"
 
@@ -441,6 +442,20 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
 // Model-level operands for the mixed path (host-side conversion, FP64 source).
 int prepare_mixed_operands(gapgpu_model& m) {
     for (Coordinate& co : m.coords) {
+        if (co.type == DESC_DISTANCE_2B) {  // FP32 sparse points and coefficients of the mixed pair kernel
+            std::vector<float> x(co.M), cf(co.M);
+            for (int s = 0; s < co.M; ++s) {
+                x[s] = (float)co.X[s];
+                cf[s] = (float)(co.alpha[s] * co.sc[s] * co.delta * co.delta);
+            }
+            GG_CUDA(cudaMalloc(&co.dXf32, sizeof(float) * std::max(co.M, 1)));
+            GG_CUDA(cudaMalloc(&co.dcoef32, sizeof(float) * std::max(co.M, 1)));
+            if (co.M > 0) {
+                GG_CUDA(cudaMemcpy(co.dXf32, x.data(), sizeof(float) * co.M, cudaMemcpyHostToDevice));
+                GG_CUDA(cudaMemcpy(co.dcoef32, cf.data(), sizeof(float) * co.M, cudaMemcpyHostToDevice));
+            }
+            continue;
+        }
         if (co.type != DESC_SOAP) continue;
         const int Dp = co.Dpad, Mp = co.Mpad;
         const size_t ne = (size_t)Mp * Dp;
