@@ -37,7 +37,8 @@ struct GeomDev {
     double lat[9], lat_eff_inv[9], lat_off[3], cutoff;
     double origin[3];     // Cartesian corner of the effective cell (non-periodic axes)
     float lat32[9];
-    float lim2;           // (cutoff + margin)^2 for the FP32 pre-filter
+    float lim2;           // (cutoff + margin)^2: FP32 distances above it are certainly outside
+    float sure2;          // (cutoff - margin)^2: FP32 distances below it are certainly inside
     int cellsN[3], img[3], pbc[3];
 };
 
@@ -85,10 +86,12 @@ __global__ void k_cell_ranges(int n, const int* __restrict__ key, int* __restric
 // One warp per atom (atoms taken in cell order for locality).  The warp walks the
 // atom's image cells in the reference's loop order; lanes take the candidates of a
 // cell 32 at a time, so the emitted order (cell-image order, then position in the
-// sorted cell) is fixed.  A candidate first passes an FP32 test on wrapped
-// coordinates with a safety margin; survivors are decided by the exact FP64 test of
-// test_form_bond (dd = pos_b - pos_a + L shift accumulated without fused multiply-add,
-// kept when sqrt(dd.dd) < cutoff).
+// sorted cell) is fixed.  A candidate is first measured in FP32 on wrapped coordinates,
+// whose error is far below the margin: beyond cutoff + margin it is out, inside
+// cutoff - margin it is in.  Only the thin band between is decided by the exact FP64
+// test of test_form_bond (dd = pos_b - pos_a + L shift accumulated without fused
+// multiply-add, kept when sqrt(dd.dd) < cutoff).  Count and fill take the same
+// decisions; the fill pass computes the FP64 displacement of every kept pair.
 // CALLER_LAYOUT (fill only): write just j and the unpacked shift (3 ints per entry)
 // into caller-owned arrays, the layout of gapgpu_neighbours; nd/ni are not written.
 template <bool FILL, bool CALLER_LAYOUT = false>
@@ -146,8 +149,11 @@ __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__
                         b = sorted[q];
                         const float4 pb = wpos[q];
                         float fx = pb.x + ox, fy = pb.y + oy, fz = pb.z + oz;
-                        bool self0 = (b == a && i4 == 0 && j4 == 0 && k4 == 0 && same_cell);
-                        if (!self0 && fx * fx + fy * fy + fz * fz < g.lim2) {
+                        const bool self0 = (b == a && i4 == 0 && j4 == 0 && k4 == 0 && same_cell);
+                        const float r2 = fx * fx + fy * fy + fz * fz;
+                        const bool sure = r2 < g.sure2;
+                        if (!FILL && sure && !self0) keep = true;
+                        else if (!self0 && r2 < g.lim2) {
                             s0 = i4 - msa0 + ms[3 * b]; s1 = j4 - msa1 + ms[3 * b + 1]; s2 = k4 - msa2 + ms[3 * b + 2];
                             d0 = __dsub_rn(pos[3 * b], pa0); d1 = __dsub_rn(pos[3 * b + 1], pa1); d2 = __dsub_rn(pos[3 * b + 2], pa2);
                             d0 = __dadd_rn(d0, __dmul_rn(g.lat[0], (double)s0)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[1], (double)s0));
@@ -156,7 +162,10 @@ __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__
                             d2 = __dadd_rn(d2, __dmul_rn(g.lat[5], (double)s1));
                             d0 = __dadd_rn(d0, __dmul_rn(g.lat[6], (double)s2)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[7], (double)s2));
                             d2 = __dadd_rn(d2, __dmul_rn(g.lat[8], (double)s2));
-                            if (!(d0 > g.cutoff || d1 > g.cutoff || d2 > g.cutoff)) {
+                            if (sure) {
+                                r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+                                keep = true;
+                            } else if (!(d0 > g.cutoff || d1 > g.cutoff || d2 > g.cutoff)) {
                                 r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
                                 keep = r < g.cutoff;
                             }
@@ -339,6 +348,7 @@ static int neighbour_geometry(int n, const double* d_pos, const double* lattice,
         for (int k = 0; k < 9; ++k) g.lat32[k] = (float)lattice[k];
         double margin = 1e-3 + 1e-6 * bsize + 1e-6 * cutoff;
         g.lim2 = (float)((cutoff + margin) * (cutoff + margin));
+        g.sure2 = cutoff > margin ? (float)((cutoff - margin) * (cutoff - margin)) : 0.0f;
     }
     return GAPGPU_OK;
 }

@@ -8,13 +8,17 @@
 //           hi*hi + hi*lo + lo*hi (three tcgen05.mma kind::f16 per k-step; the dropped
 //           lo*lo term is 2^-16 relative);
 //   tf32:   operands rounded to TF32 (cvt.rna), one tcgen05.mma kind::tf32 per k-step.
-// Structure of one CTA (128 threads, one 128x128 output tile):
+// Persistent warp-specialised kernel (one CTA of 192 threads per SM, looping over the
+// output tiles of BM=128 rows x BN columns, N-fastest so that concurrent CTAs share the
+// A row block through L2):
 //   warp 0 lane 0  TMA producer: 2-D tiled loads, 128B swizzle, into an S-stage ring
-//   warp 1 lane 0  MMA issuer: tcgen05.mma from shared-memory descriptors into TMEM,
-//                  tcgen05.commit frees each stage and finally signals the epilogue
-//   warps 0-3      epilogue: tcgen05.ld 32x32b (warp w owns TMEM lanes 32w..32w+31)
+//   warp 1         TMEM owner (512 columns: two accumulator buffers); lane 0 issues
+//                  tcgen05.mma from shared-memory descriptors, tcgen05.commit frees each
+//                  stage and hands a finished accumulator buffer to the epilogue
+//   warps 2-5      epilogue: tcgen05.ld 32x32b (warp w reads TMEM lanes 32(w%4)..+31),
+//                  overlapped with the MMAs of the next tile in the other buffer
 // Every mbarrier wait is bounded; on expiry the kernel records an error code, waits
-// (bounded) for its own work in flight, frees its TMEM and returns.
+// (bounded) for its own TMA loads and MMAs in flight, frees its TMEM and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -28,27 +32,26 @@
 namespace gapgpu {
 namespace {
 
-constexpr int BM = 128, BN = 128, THREADS = 128;
+constexpr int BM = 128, THREADS = 192;
 constexpr int MODE_BF16X3 = 1, MODE_TF32 = 2;
 constexpr int EPI_KERNEL = 1, EPI_STORE = 2;
 constexpr long long WAIT_LIMIT = 1LL << 24;
+constexpr int SMEM_BUDGET = 200 * 1024;
+constexpr int TMEM_COLS = 512;   // two accumulator buffers, ACC_STRIDE columns apart
+constexpr int ACC_STRIDE = 256;
 
-template <int MODE> struct Cfg;
-template <> struct Cfg<MODE_BF16X3> {
-    static constexpr int KB = 64;              // k elements per stage (128 bytes)
-    static constexpr int TILE_A = BM * 128;    // bytes of one A tile (hi or lo)
-    static constexpr int TILE_B = BN * 128;
-    static constexpr int STAGE = 2 * TILE_A + 2 * TILE_B;
-    static constexpr int STAGES = 3;
-    static constexpr int KSTEP = 16;           // k per tcgen05.mma
-};
-template <> struct Cfg<MODE_TF32> {
-    static constexpr int KB = 32;
+// Stage layout for one k-chunk of 128 bytes per operand row: NOPS planes (hi, lo) of A
+// (BM rows) then NOPS planes of B (BN rows).
+template <int MODE, int BN>
+struct Cfg {
+    static constexpr int KB = MODE == MODE_BF16X3 ? 64 : 32;  // k elements per stage
+    static constexpr int NOPS = MODE == MODE_BF16X3 ? 2 : 1;
     static constexpr int TILE_A = BM * 128;
     static constexpr int TILE_B = BN * 128;
-    static constexpr int STAGE = TILE_A + TILE_B;
-    static constexpr int STAGES = 6;
-    static constexpr int KSTEP = 8;
+    static constexpr int STAGE = NOPS * (TILE_A + TILE_B);
+    static constexpr int STAGES = SMEM_BUDGET / STAGE > 8 ? 8 : SMEM_BUDGET / STAGE;
+    static constexpr int KSTEP = MODE == MODE_BF16X3 ? 16 : 8;  // k per tcgen05.mma
+    static_assert(STAGES >= 2, "stage ring too small");
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -58,6 +61,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* b, int count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
 }
 __device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
     uint32_t ok;
@@ -99,7 +105,7 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
     return d;
 }
 
-template <int MODE>
+template <int MODE, int BN>
 __device__ __forceinline__ constexpr uint32_t idesc() {
     // D = F32 (bit 4); A/B format bits 7-9 / 10-12 (BF16 = 1 for kind::f16, TF32 = 2 for
     // kind::tf32); K-major A and B; N >> 3 at bits 17-22; M >> 4 at bits 24-28.
@@ -107,16 +113,16 @@ __device__ __forceinline__ constexpr uint32_t idesc() {
            ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 }
 
-template <int MODE>
+template <int MODE, int BN>
 __device__ __forceinline__ void mma(uint32_t dt, uint64_t a, uint64_t b, uint32_t acc) {
     if constexpr (MODE == MODE_BF16X3)
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
-            "l"(a), "l"(b), "r"(idesc<MODE>()), "r"(acc));
+            "l"(a), "l"(b), "r"(idesc<MODE, BN>()), "r"(acc));
     else
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
-            "l"(a), "l"(b), "r"(idesc<MODE>()), "r"(acc));
+            "l"(a), "l"(b), "r"(idesc<MODE, BN>()), "r"(acc));
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar)) : "memory");
@@ -157,28 +163,75 @@ struct EpiParams {
     int ntiles;
 };
 
+// Epilogue of one 32-column chunk for one row: kernel function and W store (EPI_KERNEL)
+// or plain FP32 store (EPI_STORE).
 template <int MODE, int EPI>
+__device__ __forceinline__ void epilogue_chunk(const EpiParams& ep, int row, int col0, const float* v, float& e_acc) {
+    if constexpr (EPI == EPI_KERNEL) {
+        float w[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float k = v[j], cf = ep.coef[col0 + j];
+            float km1;
+            if (ep.izeta == 4) km1 = k * k * k;
+            else if (ep.izeta > 0) { km1 = 1.f; for (int t = 1; t < ep.izeta; ++t) km1 *= k; }
+            else km1 = powf(k, ep.zeta - 1.f);
+            e_acc += cf * km1 * k;
+            w[j] = cf * ep.zeta * km1;
+        }
+        if constexpr (MODE == MODE_BF16X3) {
+            __nv_bfloat16 hi[32], lo[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                hi[j] = __float2bfloat16_rn(w[j]);
+                lo[j] = __float2bfloat16_rn(w[j] - __bfloat162float(hi[j]));
+            }
+            uint4* oh = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
+            uint4* ol = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(ep.out_lo) + (size_t)row * ep.ldo + col0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                oh[q] = reinterpret_cast<const uint4*>(hi)[q];
+                ol[q] = reinterpret_cast<const uint4*>(lo)[q];
+            }
+        } else {
+            float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                o[q] = make_float4(round_tf32(w[4 * q]), round_tf32(w[4 * q + 1]), round_tf32(w[4 * q + 2]),
+                                   round_tf32(w[4 * q + 3]));
+        }
+    } else {
+        float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    }
+}
+
+// C[m, n] = sum_k A[m, k] B[n, k] over m_tiles x n_tiles output tiles of BM x BN.
+template <int MODE, int EPI, int BN>
 __global__ void __launch_bounds__(THREADS, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tA0, const __grid_constant__ CUtensorMap tA1,
-              const __grid_constant__ CUtensorMap tB0, const __grid_constant__ CUtensorMap tB1, int kchunks, EpiParams ep,
-              int* err) {
-    using C = Cfg<MODE>;
+              const __grid_constant__ CUtensorMap tB0, const __grid_constant__ CUtensorMap tB1, int m_tiles, int n_tiles,
+              int kchunks, EpiParams ep, int* err) {
+    using C = Cfg<MODE, BN>;
     constexpr int S = C::STAGES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t full[S], empty[S], accum;
+    __shared__ __align__(8) uint64_t full[S], empty[S], tfull[2], tempty[2], drain;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int ntiles = m_tiles * n_tiles;
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-        mbar_init(&accum, 1);
+        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 4); }
+        mbar_init(&drain, 1);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_base)), "r"(BN));
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_base)),
+                     "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     fence_before();
@@ -188,111 +241,92 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     if (warp == 0 && lane == 0) {
         // ---------------- TMA producer
-        for (int kc = 0; kc < kchunks; ++kc) {
-            const int s = kc % S;
-            if (kc >= S && !mbar_wait(&empty[s], ((kc / S) - 1) & 1, &abort_flag, err, 1)) break;
-            unsigned char* st = smem + (size_t)s * C::STAGE;
-            mbar_expect_tx(&full[s], C::STAGE);
-            const int kx = kc * C::KB;
-            if constexpr (MODE == MODE_BF16X3) {
+        int it = 0;
+        bool ok = true;
+        for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+            const int m0 = (tile / n_tiles) * BM, n0 = (tile % n_tiles) * BN;
+            for (int kc = 0; kc < kchunks; ++kc, ++it) {
+                const int s = it % S;
+                if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1, &abort_flag, err, 1)) { ok = false; break; }
+                unsigned char* st = smem + (size_t)s * C::STAGE;
+                mbar_expect_tx(&full[s], C::STAGE);
+                const int kx = kc * C::KB;
                 tma_load(st, &tA0, kx, m0, &full[s]);
-                tma_load(st + C::TILE_A, &tA1, kx, m0, &full[s]);
-                tma_load(st + 2 * C::TILE_A, &tB0, kx, n0, &full[s]);
-                tma_load(st + 2 * C::TILE_A + C::TILE_B, &tB1, kx, n0, &full[s]);
-            } else {
-                tma_load(st, &tA0, kx, m0, &full[s]);
-                tma_load(st + C::TILE_A, &tB0, kx, n0, &full[s]);
+                if constexpr (MODE == MODE_BF16X3) tma_load(st + C::TILE_A, &tA1, kx, m0, &full[s]);
+                unsigned char* sb = st + C::NOPS * C::TILE_A;
+                tma_load(sb, &tB0, kx, n0, &full[s]);
+                if constexpr (MODE == MODE_BF16X3) tma_load(sb + C::TILE_B, &tB1, kx, n0, &full[s]);
             }
+        }
+        if (!ok) {  // let the loads already issued land before the CTA exits
+            for (int j = it - 1; j >= 0 && j >= it - S; --j)
+                mbar_wait(&full[j % S], (j / S) & 1, &abort_flag, err, 0);
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer
+        int it = 0, t = 0;
         bool ok = true;
-        for (int kc = 0; kc < kchunks && ok; ++kc) {
-            const int s = kc % S;
-            if (!mbar_wait(&full[s], (kc / S) & 1, &abort_flag, err, 2)) { ok = false; break; }
+        for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++t) {
+            const int buf = t & 1;
+            if (t >= 2 && !mbar_wait(&tempty[buf], ((t >> 1) - 1) & 1, &abort_flag, err, 2)) break;
             fence_after();
-            const uint32_t base = su32(smem + (size_t)s * C::STAGE);
+            const uint32_t acc_addr = tmem + buf * ACC_STRIDE;
+            for (int kc = 0; kc < kchunks; ++kc, ++it) {
+                const int s = it % S;
+                if (!mbar_wait(&full[s], (it / S) & 1, &abort_flag, err, 2)) { ok = false; break; }
+                fence_after();
+                const uint32_t base = su32(smem + (size_t)s * C::STAGE);
+                const uint32_t bbase = base + C::NOPS * C::TILE_A;
 #pragma unroll
-            for (int kk = 0; kk < C::KB / C::KSTEP; ++kk) {
-                const uint32_t koff = kk * 32;  // 32 bytes of K per instruction
-                const uint32_t acc = (kc > 0 || kk > 0) ? 1u : 0u;
-                if constexpr (MODE == MODE_BF16X3) {
-                    uint64_t ah = sdesc(base + koff), al = sdesc(base + C::TILE_A + koff);
-                    uint64_t bh = sdesc(base + 2 * C::TILE_A + koff), bl = sdesc(base + 2 * C::TILE_A + C::TILE_B + koff);
-                    mma<MODE>(tmem, ah, bh, acc);
-                    mma<MODE>(tmem, ah, bl, 1u);
-                    mma<MODE>(tmem, al, bh, 1u);
-                } else {
-                    uint64_t a = sdesc(base + koff), b = sdesc(base + C::TILE_A + koff);
-                    mma<MODE>(tmem, a, b, acc);
+                for (int kk = 0; kk < C::KB / C::KSTEP; ++kk) {
+                    const uint32_t koff = kk * 32;  // 32 bytes of K per instruction
+                    const uint32_t acc = (kc > 0 || kk > 0) ? 1u : 0u;
+                    if constexpr (MODE == MODE_BF16X3) {
+                        const uint64_t ah = sdesc(base + koff), al = sdesc(base + C::TILE_A + koff);
+                        const uint64_t bh = sdesc(bbase + koff), bl = sdesc(bbase + C::TILE_B + koff);
+                        mma<MODE, BN>(acc_addr, ah, bh, acc);
+                        mma<MODE, BN>(acc_addr, ah, bl, 1u);
+                        mma<MODE, BN>(acc_addr, al, bh, 1u);
+                    } else {
+                        mma<MODE, BN>(acc_addr, sdesc(base + koff), sdesc(bbase + koff), acc);
+                    }
                 }
+                mma_commit(&empty[s]);
             }
-            mma_commit(&empty[s]);
+            if (ok) mma_commit(&tfull[buf]);
         }
-        mma_commit(&accum);  // arrives once every MMA issued above has completed
-    }
-    __syncwarp();
-    // ---------------- epilogue (all 4 warps)
-    bool have = mbar_wait(&accum, 0, &abort_flag, err, 4);
-    fence_after();
-    const int row = m0 + warp * 32 + lane;
-    // tcgen05.ld is warp-collective: decide per warp
-    if (__all_sync(0xffffffffu, have && !abort_flag)) {
-        float e_acc = 0.f;
+        mma_commit(&drain);  // arrives once every MMA issued above has completed
+        mbar_wait(&drain, 0, &abort_flag, err, 0);
+    } else if (warp >= 2) {
+        // ---------------- epilogue (warps 2-5; TMEM lane quarter = warp % 4)
+        const int q = warp & 3;
+        int t = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
+            const int buf = t & 1;
+            const int m0 = (tile / n_tiles) * BM, n_blk = tile % n_tiles, n0 = n_blk * BN;
+            if (!mbar_wait(&tfull[buf], (t >> 1) & 1, &abort_flag, err, 4)) break;
+            fence_after();
+            const int row = m0 + q * 32 + lane;
+            float e_acc = 0.f;
 #pragma unroll 1
-        for (int cc = 0; cc < BN / 32; ++cc) {
-            float v[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cc * 32, v);
-            const int col0 = n0 + cc * 32;
-            if (row >= ep.rows) continue;
-            if constexpr (EPI == EPI_KERNEL) {
-                float w[32];
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    float k = v[j], cf = ep.coef[col0 + j];
-                    float km1;
-                    if (ep.izeta == 4) km1 = k * k * k;
-                    else if (ep.izeta > 0) { km1 = 1.f; for (int t = 1; t < ep.izeta; ++t) km1 *= k; }
-                    else km1 = powf(k, ep.zeta - 1.f);
-                    e_acc += cf * km1 * k;
-                    w[j] = cf * ep.zeta * km1;
-                }
-                if constexpr (MODE == MODE_BF16X3) {
-                    __nv_bfloat16 hi[32], lo[32];
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        hi[j] = __float2bfloat16_rn(w[j]);
-                        lo[j] = __float2bfloat16_rn(w[j] - __bfloat162float(hi[j]));
-                    }
-                    uint4* oh = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
-                    uint4* ol = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(ep.out_lo) + (size_t)row * ep.ldo + col0);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        oh[q] = reinterpret_cast<const uint4*>(hi)[q];
-                        ol[q] = reinterpret_cast<const uint4*>(lo)[q];
-                    }
-                } else {
-                    float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        o[q] = make_float4(round_tf32(w[4 * q]), round_tf32(w[4 * q + 1]), round_tf32(w[4 * q + 2]),
-                                           round_tf32(w[4 * q + 3]));
-                }
-            } else {
-                float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
-#pragma unroll
-                for (int q = 0; q < 8; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            for (int cc = 0; cc < BN / 32; ++cc) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_STRIDE + cc * 32, v);
+                if (row < ep.rows) epilogue_chunk<MODE, EPI>(ep, row, n0 + cc * 32, v, e_acc);
             }
-        }
-        if constexpr (EPI == EPI_KERNEL) {
-            if (row < ep.rows) ep.epart[(size_t)row * ep.ntiles + blockIdx.x] = (double)e_acc;
+            if constexpr (EPI == EPI_KERNEL) {
+                if (row < ep.rows) ep.epart[(size_t)row * ep.ntiles + n_blk] = (double)e_acc;
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[buf]);
         }
     }
     fence_before();
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 1) {
         fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
     }
 }
 
@@ -354,12 +388,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-int make_map(CUtensorMap* tm, void* base, CUtensorMapDataType dt, int esize, uint64_t inner, uint64_t outer, uint32_t box_inner) {
+int make_map(CUtensorMap* tm, void* base, CUtensorMapDataType dt, int esize, uint64_t inner, uint64_t outer, uint32_t box_inner,
+             uint32_t box_outer = BM) {
     auto enc = encode_fn();
     if (!enc) GG_FAIL(GAPGPU_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     cuuint64_t dims[2] = {inner, outer};
     cuuint64_t strides[1] = {inner * (cuuint64_t)esize};
-    cuuint32_t box[2] = {box_inner, 128};
+    cuuint32_t box[2] = {box_inner, box_outer};
     cuuint32_t es[2] = {1, 1};
     CUresult r = enc(tm, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -368,68 +403,103 @@ int make_map(CUtensorMap* tm, void* base, CUtensorMapDataType dt, int esize, uin
     return GAPGPU_OK;
 }
 
-template <int MODE, int EPI>
-int launch(gapgpu_context& c, const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0, const CUtensorMap& b1,
-           int ntile_n, int rows, int kchunks, const EpiParams& ep, int* err) {
-    using Cf = Cfg<MODE>;
+int num_sms() {
+    static int n[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 148;
+    if (!n[dev]) cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev);
+    return n[dev] > 0 ? n[dev] : 148;
+}
+
+// Widest N tile that divides N (operands are padded to multiples of 128).
+int pick_bn(int MODE, int N) {
+    if (MODE == MODE_BF16X3) return 128;  // two hi/lo planes per operand: wider tiles leave < 3 stages
+    if (N % 256 == 0) return 256;
+    if (N % 192 == 0) return 192;
+    return 128;
+}
+
+template <int MODE, int EPI, int BN>
+int launch_bn(gapgpu_context& c, const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
+              const CUtensorMap& b1, int rows, int N, int kchunks, EpiParams ep, int* err) {
+    using Cf = Cfg<MODE, BN>;
     const int smem = Cf::STAGES * Cf::STAGE + 1024;
-    GG_CUDA(cudaFuncSetAttribute(k_tc_gemm<MODE, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    dim3 grid(ntile_n, (rows + BM - 1) / BM);
-    k_tc_gemm<MODE, EPI><<<grid, THREADS, smem, c.stream>>>(a0, a1, b0, b1, kchunks, ep, err);
+    GG_CUDA(cudaFuncSetAttribute(k_tc_gemm<MODE, EPI, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const int m_tiles = (rows + BM - 1) / BM, n_tiles = N / BN;
+    if (EPI == EPI_KERNEL) ep.ntiles = n_tiles;
+    const int ntiles = m_tiles * n_tiles;
+    const int grid = std::min(ntiles, num_sms());
+    k_tc_gemm<MODE, EPI, BN><<<grid, THREADS, smem, c.stream>>>(a0, a1, b0, b1, m_tiles, n_tiles, kchunks, ep, err);
     c.launches++;
     GG_CUDA(cudaGetLastError());
     return GAPGPU_OK;
 }
 
+// One GEMM C = A B^T with the operand maps built here: A [rows x K] (planes a0, a1),
+// B [N x K] (planes b0, b1), both K-contiguous.
+template <int MODE, int EPI>
+int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows, int N, int K, EpiParams ep, int* err,
+         int* ntiles_out) {
+    const CUtensorMapDataType dt = MODE == MODE_BF16X3 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const int es = MODE == MODE_BF16X3 ? 2 : 4, KB = 128 / es;
+    const int BN = pick_bn(MODE, N);
+    CUtensorMap a0, a1, b0, b1;
+    int rc;
+    if ((rc = make_map(&a0, a0p, dt, es, K, rows, KB)) || (rc = make_map(&b0, b0p, dt, es, K, N, KB, BN))) return rc;
+    if (MODE == MODE_BF16X3) {
+        if ((rc = make_map(&a1, a1p, dt, es, K, rows, KB)) || (rc = make_map(&b1, b1p, dt, es, K, N, KB, BN))) return rc;
+    } else {
+        a1 = a0;
+        b1 = b0;
+    }
+    if (ntiles_out) *ntiles_out = N / BN;
+    const int kchunks = K / KB;
+    if (BN == 256) return launch_bn<MODE, EPI, 256>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+    if (BN == 192) return launch_bn<MODE, EPI, 192>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+    return launch_bn<MODE, EPI, 128>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+}
+
 template <int MODE>
 int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
-    using Cf = Cfg<MODE>;
     const int Dp = co.Dpad, Mp = co.Mpad;
     const size_t nq = (size_t)nc * Dp, nw = (size_t)nc * Mp;
     int rc;
-    const int ntiles = Mp / BN;
     const size_t es = MODE == MODE_BF16X3 ? 2 : 4;
+    const int ntiles_max = Mp / 128;
     if ((rc = c.Kbuf.ensure(es * nq)) || (rc = c.qlo.ensure(es * nq)) || (rc = c.Wbuf.ensure(es * nw)) ||
-        (rc = c.Wlo.ensure(es * nw)) || (rc = c.epart.ensure(sizeof(double) * (size_t)nc * ntiles)) ||
+        (rc = c.Wlo.ensure(es * nw)) || (rc = c.epart.ensure(sizeof(double) * (size_t)nc * ntiles_max)) ||
         (rc = c.Gbuf.ensure(sizeof(float) * nq)) || (rc = c.total.ensure(sizeof(int) * 4)))
         return rc;
     int* err = c.total.as<int>() + 3;
     GG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
     const int TB = 256;
     const unsigned nb = (unsigned)((nq + TB - 1) / TB);
-    CUtensorMap a0, a1, b0, b1;
-    const CUtensorMapDataType dt = MODE == MODE_BF16X3 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-    if (MODE == MODE_BF16X3) {
+    if (MODE == MODE_BF16X3)
         k_split_q<<<nb, TB, 0, c.stream>>>(nq, c.qbuf.as<float>(), c.Kbuf.as<__nv_bfloat16>(), c.qlo.as<__nv_bfloat16>());
-        if ((rc = make_map(&a0, c.Kbuf.p, dt, 2, Dp, nc, Cf::KB)) || (rc = make_map(&a1, c.qlo.p, dt, 2, Dp, nc, Cf::KB)) ||
-            (rc = make_map(&b0, co.dXhi, dt, 2, Dp, Mp, Cf::KB)) || (rc = make_map(&b1, co.dXlo, dt, 2, Dp, Mp, Cf::KB)))
-            return rc;
-    } else {
+    else
         k_round_q<<<nb, TB, 0, c.stream>>>(nq, c.qbuf.as<float>(), c.qlo.as<float>());
-        if ((rc = make_map(&a0, c.qlo.p, dt, 4, Dp, nc, Cf::KB)) || (rc = make_map(&b0, co.dXf32, dt, 4, Dp, Mp, Cf::KB)))
-            return rc;
-        a1 = a0; b1 = b0;
-    }
     c.launches++;
-    double z = co.zeta;
+    const double z = co.zeta;
     EpiParams ep{nc, Mp, co.dcoef32, (float)z, (z == std::floor(z) && z >= 1 && z <= 64) ? (int)z : 0, c.Wbuf.p, c.Wlo.p,
-                 c.epart.as<double>(), ntiles};
-    if ((rc = launch<MODE, EPI_KERNEL>(c, a0, a1, b0, b1, ntiles, nc, Dp / Cf::KB, ep, err))) return rc;
+                 c.epart.as<double>(), 0};
+    int ntiles = 0;
+    // GEMM1: K = Q X^T with the kernel epilogue (W and per-tile energies)
+    if (MODE == MODE_BF16X3)
+        rc = gemm<MODE, EPI_KERNEL>(c, c.Kbuf.p, c.qlo.p, co.dXhi, co.dXlo, nc, Mp, Dp, ep, err, &ntiles);
+    else
+        rc = gemm<MODE, EPI_KERNEL>(c, c.qlo.p, c.qlo.p, co.dXf32, co.dXf32, nc, Mp, Dp, ep, err, &ntiles);
+    if (rc) return rc;
     k_rowsum_scatter32<<<(nc + 127) / 128, 128, 0, c.stream>>>(nc, ntiles, c.epart.as<double>(), c.centres.as<int>(),
                                                               c.eatom.as<double>());
     c.launches++;
     // GEMM2: G = W X, B operand = X^T rows (k = sparse index contiguous)
-    if (MODE == MODE_BF16X3) {
-        if ((rc = make_map(&a0, c.Wbuf.p, dt, 2, Mp, nc, Cf::KB)) || (rc = make_map(&a1, c.Wlo.p, dt, 2, Mp, nc, Cf::KB)) ||
-            (rc = make_map(&b0, co.dXThi, dt, 2, Mp, Dp, Cf::KB)) || (rc = make_map(&b1, co.dXTlo, dt, 2, Mp, Dp, Cf::KB)))
-            return rc;
-    } else {
-        if ((rc = make_map(&a0, c.Wbuf.p, dt, 4, Mp, nc, Cf::KB)) || (rc = make_map(&b0, co.dXTf32, dt, 4, Mp, Dp, Cf::KB)))
-            return rc;
-        a1 = a0; b1 = b0;
-    }
     EpiParams ep2{nc, Dp, nullptr, 0.f, 0, c.Gbuf.p, nullptr, nullptr, 0};
-    if ((rc = launch<MODE, EPI_STORE>(c, a0, a1, b0, b1, Dp / BN, nc, Mp / Cf::KB, ep2, err))) return rc;
+    if (MODE == MODE_BF16X3)
+        rc = gemm<MODE, EPI_STORE>(c, c.Wbuf.p, c.Wlo.p, co.dXThi, co.dXTlo, nc, Dp, Mp, ep2, err, nullptr);
+    else
+        rc = gemm<MODE, EPI_STORE>(c, c.Wbuf.p, c.Wbuf.p, co.dXTf32, co.dXTf32, nc, Dp, Mp, ep2, err, nullptr);
+    if (rc) return rc;
     int herr = 0;
     GG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     GG_CUDA(cudaStreamSynchronize(c.stream));
@@ -494,7 +564,7 @@ int prepare_mixed_operands(gapgpu_model& m) {
 int gp_mixed(gapgpu_context& c, const Coordinate& co, int nc, int precision) {
     if (nc == 0) return GAPGPU_OK;
     if (co.cov != COV_DOT_PRODUCT) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP coordinates need the dot_product covariance");
-    if (co.Dpad % BN || co.Mpad % BN) GG_FAIL(GAPGPU_ERR_ARG, "internal: operand padding is not a multiple of 128");
+    if (co.Dpad % 128 || co.Mpad % 128) GG_FAIL(GAPGPU_ERR_ARG, "internal: operand padding is not a multiple of 128");
     return precision == GAPGPU_MIXED_BF16X3 ? run_mixed<MODE_BF16X3>(c, co, nc) : run_mixed<MODE_TF32>(c, co, nc);
 }
 
