@@ -100,6 +100,48 @@ int gapgpu_calc(gapgpu_context* ctx, int n, const double* pos, const int32_t* Z,
 int gapgpu_calc_device(gapgpu_context* ctx, int n, const double* d_pos, const int32_t* d_Z, const double* lattice,
                        const int32_t* pbc, double* d_energy, double* d_force, double* d_virial);
 
+/* Batched evaluation of many independent structures in one pass (one neighbour build,
+ * one SOAP/GEMM pipeline over every centre of the batch, per-structure reductions):
+ * the loop over frames of quip / quippy's calculate over a list of Atoms
+ * (quippy/quippy/potential.py:177-325) done as one GPU evaluation.  Structures are
+ * concatenated: n_atoms[s] atoms each, pos double[3*sum n] and Z int32[sum n] in that
+ * order, lattices double[9*nstruct] (columns are cell vectors), pbcs int32[3*nstruct].
+ * Outputs (nullable): energies[nstruct], forces double[3*sum n], virials
+ * double[9*nstruct].  Each structure's results are bit-identical to evaluating it alone
+ * with the same context settings. */
+int gapgpu_calc_batch(gapgpu_context* ctx, int nstruct, const int32_t* n_atoms, const double* pos, const int32_t* Z,
+                      const double* lattices, const int32_t* pbcs, double* energies, double* forces, double* virials,
+                      const char* args);
+
+/* Context options: "graphs" (0/1): replay the evaluation phase from a CUDA graph when a
+ * call has the same shapes and buffers as the previous one (captured on the second such
+ * call); "timing" (0/1): per-stage CUDA events (gapgpu_context_timings). */
+int gapgpu_context_set_option(gapgpu_context* ctx, const char* key, int value);
+
+/* Device memory one evaluation of n_atoms atoms with about mean_neighbours neighbours
+ * each needs in a context of this precision (bytes, an estimate used for admission). */
+int gapgpu_model_footprint(const gapgpu_model* model, int precision, int64_t n_atoms, double mean_neighbours,
+                           int64_t* bytes);
+
+/* Device-resident velocity-Verlet MD of nstruct independent replicas
+ * (DynamicalSystem advance_verlet1/advance_verlet2, src/libAtoms/DynamicalSystem.f95:
+ * 1814-2383, as run by DynamicalSystem_run, src/Potentials/Potential.f95:2304-2370),
+ * with QUIP's skin rule for the connection (Connection.f95:1086-1125): lists are built
+ * at cutoff + skin and refreshed (connection_calc_dists) until an atom has moved skin/2.
+ * Layouts as gapgpu_calc_batch; velo in A/fs, mass per atom in eV fs^2/A^2 (amu times
+ * MASSCONVERT), dt in fs.  The object owns its own context (gapgpu_md_context). */
+typedef struct gapgpu_md gapgpu_md;
+int gapgpu_md_create(const gapgpu_model* model, int precision, int nstruct, const int32_t* n_atoms, const double* pos,
+                     const double* velo, const double* mass, const int32_t* Z, const double* lattices,
+                     const int32_t* pbcs, double dt, double skin, gapgpu_md** out);
+int gapgpu_md_step(gapgpu_md* md, int nsteps);
+/* Current positions, velocities, forces (nullable host arrays) and per-replica
+ * potential energies and virials. */
+int gapgpu_md_state(gapgpu_md* md, double* pos, double* velo, double* force, double* energies, double* virials);
+int gapgpu_md_counters(const gapgpu_md* md, int64_t* steps, int64_t* rebuilds, int64_t* graph_replays);
+gapgpu_context* gapgpu_md_context(gapgpu_md* md);
+void gapgpu_md_destroy(gapgpu_md* md);
+
 /* Wait for the context's stream. */
 int gapgpu_context_sync(gapgpu_context* ctx);
 

@@ -18,7 +18,9 @@ PRECISIONS = {"fp64": FP64, "bf16x3": MIXED_BF16X3, "tf32": MIXED_TF32}
 EXPORTS = ["gapgpu_last_error", "gapgpu_model_create", "gapgpu_model_cutoff", "gapgpu_model_info",
            "gapgpu_model_destroy", "gapgpu_context_create", "gapgpu_context_set_stream", "gapgpu_context_destroy",
            "gapgpu_calc", "gapgpu_calc_device", "gapgpu_context_sync", "gapgpu_neighbours", "gapgpu_descriptors",
-           "gapgpu_context_timings", "gapgpu_context_launches", "gapgpu_neighbours_static"]
+           "gapgpu_context_timings", "gapgpu_context_launches", "gapgpu_neighbours_static", "gapgpu_calc_batch",
+           "gapgpu_context_set_option", "gapgpu_model_footprint", "gapgpu_md_create", "gapgpu_md_step", "gapgpu_md_state",
+           "gapgpu_md_counters", "gapgpu_md_context", "gapgpu_md_destroy"]
 
 
 class GapGpuError(RuntimeError):
@@ -64,6 +66,19 @@ def load(build_if_missing=True):
                                            i64, P(i64), c_void_p]
     L.gapgpu_descriptors.argtypes = [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, i64,
                                      P(c_int)]
+    L.gapgpu_calc_batch.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p, c_char_p]
+    L.gapgpu_context_set_option.argtypes = [c_void_p, c_char_p, c_int]
+    L.gapgpu_model_footprint.argtypes = [c_void_p, c_int, i64, c_double, P(i64)]
+    L.gapgpu_md_create.argtypes = [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_double, c_double, P(c_void_p)]
+    L.gapgpu_md_step.argtypes = [c_void_p, c_int]
+    L.gapgpu_md_state.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+    L.gapgpu_md_counters.argtypes = [c_void_p, P(i64), P(i64), P(i64)]
+    L.gapgpu_md_context.argtypes = [c_void_p]
+    L.gapgpu_md_context.restype = c_void_p
+    L.gapgpu_md_destroy.argtypes = [c_void_p]
+    L.gapgpu_md_destroy.restype = None
     L.gapgpu_context_timings.argtypes = [c_void_p, P(c_double), c_int]
     L.gapgpu_context_launches.argtypes = [c_void_p, P(i64)]
     _lib = L

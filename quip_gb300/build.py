@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgapgpu.so")
-SOURCES = ["model.cpp", "neighbours.cu", "soap.cu", "gp64.cu", "tcgen05.cu", "pair.cu", "calc.cu"]
+SOURCES = ["model.cpp", "neighbours.cu", "soap.cu", "gp64.cu", "tcgen05.cu", "pair.cu", "calc.cu", "md.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-Xcompiler", "-Wall"]
 

@@ -21,11 +21,6 @@ namespace {
 
 size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
 
-__global__ void k_f64_to_f32(size_t n, const double* __restrict__ a, float* __restrict__ b) {
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
-}
-
 struct ArgOpts {
     int precision = -1;
     bool bad_scale = false;
@@ -66,26 +61,14 @@ int check_device() {
     return GAPGPU_OK;
 }
 
-struct StageTimer {
-    gapgpu_context& c;
-    int k = 0;
-    explicit StageTimer(gapgpu_context& c_) : c(c_) {
-        if (!c.events) {
-            for (auto& e : c.ev) cudaEventCreate(&e);
-            c.events = true;
-        }
-    }
-    void mark() {
-        if (k < 8) cudaEventRecord(c.ev[k++], c.stream);
-    }
-};
-
 }  // namespace
 
 int upload_model(gapgpu_model& m) {
     int rc;
     if ((rc = check_device())) return rc;
     cudaGetDevice(&m.device);
+    GG_CUDA(cudaMalloc(&m.de0, sizeof(double) * 128));
+    GG_CUDA(cudaMemcpy(m.de0, m.e0, sizeof(double) * 128, cudaMemcpyHostToDevice));
     for (Coordinate& co : m.coords) {
         co.Dpad = (int)round_up(co.D, 128);
         co.Mpad = (int)round_up(co.M, 128);
@@ -110,6 +93,8 @@ int upload_model(gapgpu_model& m) {
 }
 
 void free_model_device(gapgpu_model& m) {
+    if (m.de0) cudaFree(m.de0);
+    m.de0 = nullptr;
     for (Coordinate& co : m.coords) {
         for (void* p : {(void*)co.dX64, (void*)co.dcoef, (void*)co.dXf32, (void*)co.dXhi, (void*)co.dXlo, (void*)co.dXTf32,
                         (void*)co.dXThi, (void*)co.dXTlo, (void*)co.dcoef32, (void*)co.dtheta, co.dtab[0], co.dtab[1]})
@@ -122,66 +107,196 @@ void free_model_device(gapgpu_model& m) {
 
 int prepare_mixed_operands(gapgpu_model& m);  // tcgen05.cu
 
-// The whole pipeline on device-resident positions (c.pos, c.Z, optional mask).
-static int run_pipeline(gapgpu_context& c, int n, const double* lattice, const int* pbc, const int* d_mask, int precision) {
+namespace {
+constexpr int RED_CHUNK = 4096;  // atoms per first-level reduction block (relative to each structure's first atom)
+}
+
+// ---------------------------------------------------------------- phase A
+// Neighbour list (rebuilt at `cutoff`, or only its displacements refreshed when the
+// list is kept), per-coordinate centre lists, segmented-reduction tables and the
+// output buffers.  All host synchronisation of an evaluation happens here.
+int prepare(gapgpu_context& c, int nstruct, const int* n_atoms, const double* lattices, const int* pbcs, const int* d_mask,
+            double cutoff, bool rebuild) {
     const gapgpu_model& m = *c.model;
-    int rc;
-    StageTimer tm(c);
-    tm.mark();
-    if ((rc = build_neighbours(c, n, c.pos.as<double>(), lattice, pbc, m.cutoff, nullptr))) return rc;
-    tm.mark();
-    const size_t P = std::max<long long>(c.n_pairs, 1);
-    if ((rc = c.fpair.ensure(sizeof(double) * 3 * P)) || (rc = c.epair.ensure(sizeof(double) * P)) ||
-        (rc = c.eatom.ensure(sizeof(double) * std::max(n, 1))))
-        return rc;
-    GG_CUDA(cudaMemsetAsync(c.fpair.p, 0, sizeof(double) * 3 * P, c.stream));
-    GG_CUDA(cudaMemsetAsync(c.epair.p, 0, sizeof(double) * P, c.stream));
-    GG_CUDA(cudaMemsetAsync(c.eatom.p, 0, sizeof(double) * std::max(n, 1), c.stream));
-    const int saved = c.precision;
-    c.precision = precision;
-    float t_fwd = 0, t_gemm = 0, t_bwd = 0, t_2b = 0;
-    cudaEvent_t e0, e1, e2, e3;
-    cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&e2); cudaEventCreate(&e3);
-    for (const Coordinate& co : m.coords) {
-        if (co.type == DESC_SOAP) {
-            int nc = 0;
-            if ((rc = select_centres(c, co, n, d_mask, &nc))) break;
-            cudaEventRecord(e0, c.stream);
-            if ((rc = soap_forward(c, co, n, nc))) break;
-            cudaEventRecord(e1, c.stream);
-            rc = precision == GAPGPU_FP64 ? gp_fp64(c, co, nc) : gp_mixed(c, co, nc, precision);
-            if (rc) break;
-            cudaEventRecord(e2, c.stream);
-            if ((rc = soap_backward(c, co, n, nc))) break;
-            cudaEventRecord(e3, c.stream);
-            cudaEventSynchronize(e3);
-            float a, b, d;
-            cudaEventElapsedTime(&a, e0, e1); cudaEventElapsedTime(&b, e1, e2); cudaEventElapsedTime(&d, e2, e3);
-            t_fwd += a; t_gemm += b; t_bwd += d;
-        } else {
-            cudaEventRecord(e0, c.stream);
-            if ((rc = pair_2b(c, co, n, d_mask))) break;
-            cudaEventRecord(e1, c.stream);
-            cudaEventSynchronize(e1);
-            float a;
-            cudaEventElapsedTime(&a, e0, e1);
-            t_2b += a;
+    int rc, n = 0;
+    for (int s = 0; s < nstruct; ++s) n += n_atoms[s];
+    const double* d_pos = c.pos.as<double>();
+    c.nbr_timed = c.timed;
+    if (c.timed) {
+        for (cudaEvent_t& e : c.nev)
+            if (!e) cudaEventCreate(&e);
+        cudaEventRecord(c.nev[0], c.stream);
+    }
+    if (rebuild) {
+        if ((rc = build_neighbours_batch(c, nstruct, n_atoms, d_pos, lattices, pbcs, cutoff))) return rc;
+    } else {
+        if (n != c.n_total || nstruct != c.nstruct) GG_FAIL(GAPGPU_ERR_ARG, "kept neighbour list does not match the atoms");
+        if ((rc = refresh_distances(c, d_pos))) return rc;
+    }
+    if (c.timed) cudaEventRecord(c.nev[1], c.stream);
+    if (!rebuild) return GAPGPU_OK;  // centres, tables and buffers are those of the build
+    c.nstruct = nstruct;
+    c.n_total = n;
+    const int ncoord = (int)m.coords.size();
+    if ((rc = c.centres.ensure(sizeof(int) * std::max<size_t>(1, (size_t)n * ncoord)))) return rc;
+    c.nc_coord.assign(ncoord, 0);
+    for (int k = 0; k < ncoord; ++k) {
+        const Coordinate& co = m.coords[k];
+        if (co.type != DESC_SOAP || n == 0) continue;
+        c.cur_centres = c.centres.as<int>() + (size_t)k * n;
+        if ((rc = select_centres(c, co, n, d_mask, &c.nc_coord[k]))) return rc;
+    }
+    // reduction tables: chunks of RED_CHUNK atoms counted from each structure's first atom
+    c.h_chunks.clear();
+    c.h_schunk.assign(nstruct + 1, 0);
+    for (int s = 0, a0 = 0; s < nstruct; a0 += n_atoms[s], ++s) {
+        c.h_schunk[s] = (int)c.h_chunks.size() / 2;
+        for (int a = a0; a < a0 + n_atoms[s]; a += RED_CHUNK) {
+            c.h_chunks.push_back(a);
+            c.h_chunks.push_back(std::min(a0 + n_atoms[s], a + RED_CHUNK));
         }
     }
-    cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2); cudaEventDestroy(e3);
-    c.precision = saved;
-    if (rc) return rc;
-    tm.mark();
-    if ((rc = gather_outputs(c, m, n, d_mask))) return rc;
-    tm.mark();
+    c.h_schunk[nstruct] = (int)c.h_chunks.size() / 2;
+    const size_t nch = std::max<size_t>(1, c.h_chunks.size() / 2);
+    const size_t P = std::max<long long>(c.n_pairs, 1);
+    if ((rc = c.chunks.ensure(sizeof(int2) * nch)) || (rc = c.schunk.ensure(sizeof(int) * (nstruct + 1))) ||
+        (rc = c.redpart.ensure(sizeof(double) * 10 * nch)) || (rc = c.fpair.ensure(sizeof(double) * 3 * P)) ||
+        (rc = c.epair.ensure(sizeof(double) * P)) || (rc = c.eatom.ensure(sizeof(double) * std::max(n, 1))) ||
+        (rc = c.out_le.ensure(sizeof(double) * std::max(n, 1))) || (rc = c.out_f.ensure(sizeof(double) * 3 * std::max(n, 1))) ||
+        (rc = c.out_lv.ensure(sizeof(double) * 9 * std::max(n, 1))) || (rc = c.out_e.ensure(sizeof(double) * 10 * nstruct)) ||
+        (rc = c.total.ensure(sizeof(int) * 4)))
+        return rc;
+    if (!c.h_chunks.empty())
+        GG_CUDA(cudaMemcpyAsync(c.chunks.p, c.h_chunks.data(), sizeof(int) * c.h_chunks.size(), cudaMemcpyHostToDevice,
+                                c.stream));
+    GG_CUDA(cudaMemcpyAsync(c.schunk.p, c.h_schunk.data(), sizeof(int) * (nstruct + 1), cudaMemcpyHostToDevice, c.stream));
+    // the host vectors above must outlive the copies
+    GG_CUDA(cudaStreamSynchronize(c.stream));
+    return GAPGPU_OK;
+}
+
+namespace {
+
+void record(gapgpu_context& c, bool timed) {
+    if (!timed || c.ncev >= 64) return;
+    if (!c.cev[c.ncev]) cudaEventCreate(&c.cev[c.ncev]);
+    cudaEventRecord(c.cev[c.ncev++], c.stream);
+}
+
+// ---------------------------------------------------------------- phase B
+// Stream work only (kernels, memsets): the part of an evaluation that a CUDA graph can
+// capture.  With `timed`, events bracket the stages: [start] then per coordinate
+// (fwd, gemm, bwd | pair) and [gather, end].
+int evaluate(gapgpu_context& c, int precision, const int* d_mask, bool timed) {
+    const gapgpu_model& m = *c.model;
+    const int n = c.n_total;
+    int rc = GAPGPU_OK;
+    c.ncev = 0;
+    record(c, timed);
+    GG_CUDA(cudaMemsetAsync(c.total.as<int>() + 3, 0, sizeof(int), c.stream));
+    if (n > 0) {
+        const size_t P = std::max<long long>(c.n_pairs, 1);
+        GG_CUDA(cudaMemsetAsync(c.fpair.p, 0, sizeof(double) * 3 * P, c.stream));
+        GG_CUDA(cudaMemsetAsync(c.epair.p, 0, sizeof(double) * P, c.stream));
+        GG_CUDA(cudaMemsetAsync(c.eatom.p, 0, sizeof(double) * n, c.stream));
+        const int saved = c.precision;
+        c.precision = precision;
+        for (int k = 0; k < (int)m.coords.size() && !rc; ++k) {
+            const Coordinate& co = m.coords[k];
+            if (co.type == DESC_SOAP) {
+                const int nc = c.nc_coord[k];
+                c.cur_centres = c.centres.as<int>() + (size_t)k * n;
+                record(c, timed);
+                if ((rc = soap_forward(c, co, n, nc))) break;
+                record(c, timed);
+                rc = precision == GAPGPU_FP64 ? gp_fp64(c, co, nc) : gp_mixed(c, co, nc, precision);
+                if (rc) break;
+                record(c, timed);
+                if ((rc = soap_backward(c, co, n, nc))) break;
+            } else {
+                record(c, timed);
+                if ((rc = pair_2b(c, co, n, d_mask))) break;
+            }
+        }
+        c.precision = saved;
+        if (rc) return rc;
+        record(c, timed);
+        if ((rc = gather_outputs(c, m, n, d_mask))) return rc;
+    } else {
+        GG_CUDA(cudaMemsetAsync(c.out_e.p, 0, sizeof(double) * 10 * c.nstruct, c.stream));
+    }
+    record(c, timed);
     GG_CUDA(cudaGetLastError());
-    cudaEventSynchronize(c.ev[3]);
-    float a = 0, b = 0, d = 0;
-    cudaEventElapsedTime(&a, c.ev[0], c.ev[1]);
-    cudaEventElapsedTime(&b, c.ev[2], c.ev[3]);
-    cudaEventElapsedTime(&d, c.ev[0], c.ev[3]);
-    c.t.neighbours = a; c.t.reduce = b; c.t.total = d;
-    c.t.soap_fwd = t_fwd; c.t.gemm = t_gemm; c.t.soap_bwd = t_bwd; c.t.pair2b = t_2b;
+    return GAPGPU_OK;
+}
+
+std::vector<uintptr_t> graph_key(const gapgpu_context& c, int precision, const int* d_mask) {
+    std::vector<uintptr_t> k = {(uintptr_t)precision, (uintptr_t)d_mask, (uintptr_t)c.n_total, (uintptr_t)c.nstruct,
+                                (uintptr_t)c.n_pairs, (uintptr_t)c.model, (uintptr_t)c.stream,
+                                (uintptr_t)c.h_chunks.size()};
+    for (int nc : c.nc_coord) k.push_back((uintptr_t)nc);
+    for (const gapgpu::DBuf* b : c.buffers()) k.push_back((uintptr_t)b->p);
+    return k;
+}
+
+}  // namespace
+
+// Phase B, replayed from a CUDA graph when the context's graph mode is on and the same
+// shapes and buffers were seen on the previous call (capture on the second identical
+// call, replay from the third).
+int run_evaluation(gapgpu_context& c, int precision, const int* d_mask) {
+    c.stage_valid = false;
+    if (!c.graph_mode) {
+        int rc = evaluate(c, precision, d_mask, c.timed);
+        c.stage_valid = c.timed;
+        return rc;
+    }
+    std::vector<uintptr_t> key = graph_key(c, precision, d_mask);
+    if (c.graph && key == c.graph_key) {
+        GG_CUDA(cudaGraphLaunch(c.graph, c.stream));
+        c.launches += c.graph_launches;
+        c.graph_hits++;
+        return GAPGPU_OK;
+    }
+    if (key == c.last_key) {
+        if (c.graph) {
+            cudaGraphExecDestroy(c.graph);
+            c.graph = nullptr;
+        }
+        const long long l0 = c.launches;
+        GG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed));
+        int rc = evaluate(c, precision, d_mask, false);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) GG_FAIL(GAPGPU_ERR_CUDA, std::string("CUDA graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            c.graph = nullptr;
+            GG_FAIL(GAPGPU_ERR_CUDA, std::string("CUDA graph instantiate: ") + cudaGetErrorString(e));
+        }
+        c.graph_key = key;
+        c.graph_launches = c.launches - l0;
+        GG_CUDA(cudaGraphLaunch(c.graph, c.stream));
+        return GAPGPU_OK;
+    }
+    c.last_key = key;
+    int rc = evaluate(c, precision, d_mask, c.timed);
+    c.stage_valid = c.timed;
+    return rc;
+}
+
+// Error bits left on the device by the last evaluation (overlapping atoms found by a
+// distance refresh, an expired tensor-core wait); call after the stream is idle.
+int check_device_flags(gapgpu_context& c) {
+    int f[4] = {0, 0, 0, 0};
+    GG_CUDA(cudaMemcpy(f, c.total.p, sizeof f, cudaMemcpyDeviceToHost));
+    if (f[2] & 2) GG_FAIL(GAPGPU_ERR_ATOMS, "connection_calc_dists: atoms overlap exactly (distance below 1e-10)");
+    if (f[3]) GG_FAIL(GAPGPU_ERR_TIMEOUT, "tensor-core GEMM: a bounded mbarrier wait expired (code " + std::to_string(f[3]) + ")");
     return GAPGPU_OK;
 }
 
@@ -190,15 +305,65 @@ static int run_pipeline(gapgpu_context& c, int n, const double* lattice, const i
 using namespace gapgpu;
 
 gapgpu_context::~gapgpu_context() {
-    for (DBuf* b : {&pos, &Z, &mask, &out_e, &out_f, &out_v, &out_le, &out_lv, &cell_key, &cell_key2, &atom_idx, &atom_idx2,
-                    &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev, &nbr_i, &wpos,
-                    &total, &fpair, &epair, &eatom, &redpart, &flags, &centres, &ncent, &coef, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf,
-                    &Wlo, &epart, &ecent, &Gbuf, &scratch})
-        b->release();
-    if (events)
-        for (auto& e : ev) cudaEventDestroy(e);
+    for (DBuf* b : buffers()) b->release();
+    for (cudaEvent_t e : nev)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : cev)
+        if (e) cudaEventDestroy(e);
+    if (graph) cudaGraphExecDestroy(graph);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
+
+namespace {
+
+// Stage times of the last timed evaluation, from its events (waits for them).
+void compute_timings(gapgpu_context& c) {
+    Timings t;
+    if (c.stage_valid && c.ncev >= 2) {
+        cudaEventSynchronize(c.cev[c.ncev - 1]);
+        auto el = [&](cudaEvent_t a, cudaEvent_t b) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, a, b);
+            return ms;
+        };
+        int i = 1;
+        t.reduce += el(c.cev[0], c.cev[1]);  // output zeroing
+        for (const Coordinate& co : c.model->coords) {
+            if (co.type == DESC_SOAP) {
+                if (i + 3 >= c.ncev) break;
+                t.soap_fwd += el(c.cev[i], c.cev[i + 1]);
+                t.gemm += el(c.cev[i + 1], c.cev[i + 2]);
+                t.soap_bwd += el(c.cev[i + 2], c.cev[i + 3]);
+                i += 3;
+            } else {
+                if (i + 1 >= c.ncev) break;
+                t.pair2b += el(c.cev[i], c.cev[i + 1]);
+                i += 1;
+            }
+        }
+        if (i + 1 < c.ncev) t.reduce += el(c.cev[i], c.cev[i + 1]);
+        t.total = el(c.cev[0], c.cev[c.ncev - 1]);
+        if (c.nbr_timed) {
+            t.neighbours = el(c.nev[0], c.nev[1]);
+            t.total = el(c.nev[0], c.cev[c.ncev - 1]);
+        }
+    }
+    c.t = t;
+}
+
+int copy_inputs(gapgpu_context& c, int n, const double* pos, const int32_t* Z, const int32_t* mask, cudaMemcpyKind kind) {
+    int rc;
+    if ((rc = c.pos.ensure(sizeof(double) * 3 * std::max(n, 1))) || (rc = c.Z.ensure(sizeof(int) * std::max(n, 1))) ||
+        (rc = c.mask.ensure(sizeof(int) * std::max(n, 1))))
+        return rc;
+    if (n == 0) return GAPGPU_OK;
+    GG_CUDA(cudaMemcpyAsync(c.pos.p, pos, sizeof(double) * 3 * n, kind, c.stream));
+    GG_CUDA(cudaMemcpyAsync(c.Z.p, Z, sizeof(int) * n, kind, c.stream));
+    if (mask) GG_CUDA(cudaMemcpyAsync(c.mask.p, mask, sizeof(int) * n, kind, c.stream));
+    return GAPGPU_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -223,6 +388,27 @@ int gapgpu_model_create(const char* xml, size_t xml_len, const char* init_args, 
 int gapgpu_model_cutoff(const gapgpu_model* m, double* cutoff) {
     if (!m || !cutoff) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_model_cutoff: NULL argument");
     *cutoff = m->cutoff;
+    return GAPGPU_OK;
+}
+
+int gapgpu_model_footprint(const gapgpu_model* m, int precision, int64_t n_atoms, double mean_neighbours, int64_t* bytes) {
+    if (!m || !bytes || n_atoms < 0 || !(mean_neighbours >= 0)) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_model_footprint: bad argument");
+    const double rs = precision == GAPGPU_FP64 ? 8.0 : 4.0;
+    // per atom: positions, species, outputs, cell binning; per pair: list (j, d, shift,
+    // reverse, i) and force/energy accumulators
+    double per_atom = 3 * 8 + 4 + 8 * (1 + 3 + 9 + 1) + 7 * 4 + 16 + mean_neighbours * (4 + 32 + 4 + 4 + 4 + 24 + 8);
+    double per_centre = 0;
+    for (const Coordinate& co : m->coords) {
+        if (co.type != DESC_SOAP) continue;
+        const SoapParams& sp = co.soap;
+        const double ncomp = (double)sp.n_species * sp.n_max * (sp.l_max + 1) * (sp.l_max + 1);
+        const double Dp = ((co.D + 127) / 128) * 128.0, Mp = ((co.M + 127) / 128) * 128.0;
+        double c = rs * (ncomp + 2 * Dp) + 8 + 4;          // c, q, G, norm, centre index
+        if (precision == GAPGPU_FP64) c += 8 * Mp + 8 * (Mp / 64 + 1) + 8;
+        else c += 2 * 4 * Dp + 2 * 4 * Mp + 8 * (Mp / 128);  // GEMM operands (hi/lo or TF32), W, tile sums
+        per_centre = std::max(per_centre, c);              // coordinates run one after the other
+    }
+    *bytes = (int64_t)((per_atom + per_centre) * (double)n_atoms) + (64 << 20);
     return GAPGPU_OK;
 }
 
@@ -268,6 +454,15 @@ int gapgpu_context_set_stream(gapgpu_context* c, void* s) {
     return GAPGPU_OK;
 }
 
+int gapgpu_context_set_option(gapgpu_context* c, const char* key, int value) {
+    if (!c || !key) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_set_option: NULL argument");
+    const std::string k(key);
+    if (k == "graphs") c->graph_mode = value ? 1 : 0;
+    else if (k == "timing") c->timed = value != 0;
+    else GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_set_option: unknown option " + k);
+    return GAPGPU_OK;
+}
+
 void gapgpu_context_destroy(gapgpu_context* c) { delete c; }
 
 int gapgpu_context_sync(gapgpu_context* c) {
@@ -290,17 +485,10 @@ int gapgpu_calc(gapgpu_context* c, int n, const double* pos, const int32_t* Z, c
         if (virial) std::memset(virial, 0, 9 * sizeof(double));
         return GAPGPU_OK;
     }
-    if ((rc = c->pos.ensure(sizeof(double) * 3 * n)) || (rc = c->Z.ensure(sizeof(int) * n)) ||
-        (rc = c->mask.ensure(sizeof(int) * n)))
-        return rc;
-    GG_CUDA(cudaMemcpyAsync(c->pos.p, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
-    GG_CUDA(cudaMemcpyAsync(c->Z.p, Z, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
-    const int* dmask = nullptr;
-    if (atom_mask) {
-        GG_CUDA(cudaMemcpyAsync(c->mask.p, atom_mask, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
-        dmask = c->mask.as<int>();
-    }
-    if ((rc = run_pipeline(*c, n, lattice, pbc, dmask, prec))) return rc;
+    if ((rc = copy_inputs(*c, n, pos, Z, atom_mask, cudaMemcpyHostToDevice))) return rc;
+    const int* dmask = atom_mask ? c->mask.as<int>() : nullptr;
+    if ((rc = prepare(*c, 1, &n, lattice, pbc, dmask, c->model->cutoff, true))) return rc;
+    if ((rc = run_evaluation(*c, prec, dmask))) return rc;
     double red[10];
     GG_CUDA(cudaMemcpyAsync(red, c->out_e.p, sizeof red, cudaMemcpyDeviceToHost, c->stream));
     if (force) GG_CUDA(cudaMemcpyAsync(force, c->out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
@@ -308,6 +496,7 @@ int gapgpu_calc(gapgpu_context* c, int n, const double* pos, const int32_t* Z, c
     if (local_virial)
         GG_CUDA(cudaMemcpyAsync(local_virial, c->out_lv.p, sizeof(double) * 9 * n, cudaMemcpyDeviceToHost, c->stream));
     GG_CUDA(cudaStreamSynchronize(c->stream));
+    if ((rc = check_device_flags(*c))) return rc;
     if (energy) *energy = red[0];
     if (virial) std::memcpy(virial, red + 1, 9 * sizeof(double));
     return GAPGPU_OK;
@@ -318,14 +507,45 @@ int gapgpu_calc_device(gapgpu_context* c, int n, const double* d_pos, const int3
     if (!c || n <= 0 || !d_pos || !d_Z || !lattice || !pbc) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_device: bad argument");
     c->launches = 0;
     int rc;
-    if ((rc = c->pos.ensure(sizeof(double) * 3 * n)) || (rc = c->Z.ensure(sizeof(int) * n))) return rc;
-    GG_CUDA(cudaMemcpyAsync(c->pos.p, d_pos, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, c->stream));
-    GG_CUDA(cudaMemcpyAsync(c->Z.p, d_Z, sizeof(int) * n, cudaMemcpyDeviceToDevice, c->stream));
-    if ((rc = run_pipeline(*c, n, lattice, pbc, nullptr, c->precision))) return rc;
+    if ((rc = copy_inputs(*c, n, d_pos, d_Z, nullptr, cudaMemcpyDeviceToDevice))) return rc;
+    if ((rc = prepare(*c, 1, &n, lattice, pbc, nullptr, c->model->cutoff, true))) return rc;
+    if ((rc = run_evaluation(*c, c->precision, nullptr))) return rc;
     if (d_energy) GG_CUDA(cudaMemcpyAsync(d_energy, c->out_e.p, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     if (d_virial)
         GG_CUDA(cudaMemcpyAsync(d_virial, c->out_e.as<double>() + 1, 9 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     if (d_force) GG_CUDA(cudaMemcpyAsync(d_force, c->out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, c->stream));
+    return GAPGPU_OK;
+}
+
+int gapgpu_calc_batch(gapgpu_context* c, int nstruct, const int32_t* n_atoms, const double* pos, const int32_t* Z,
+                      const double* lattices, const int32_t* pbcs, double* energies, double* forces, double* virials,
+                      const char* args) {
+    if (!c || nstruct < 1 || !n_atoms || !lattices || !pbcs) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_batch: bad argument");
+    c->launches = 0;
+    ArgOpts o;
+    int rc;
+    if ((rc = parse_calc_args(args, o))) return rc;
+    const int prec = o.precision >= 0 ? o.precision : c->precision;
+    long long n = 0;
+    for (int s = 0; s < nstruct; ++s) {
+        if (n_atoms[s] < 0) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_batch: negative atom count");
+        n += n_atoms[s];
+    }
+    if (n > (1LL << 30)) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_batch: too many atoms");
+    if (n > 0 && (!pos || !Z)) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_batch: NULL positions or species");
+    if ((rc = copy_inputs(*c, (int)n, pos, Z, nullptr, cudaMemcpyHostToDevice))) return rc;
+    if ((rc = prepare(*c, nstruct, n_atoms, lattices, pbcs, nullptr, c->model->cutoff, true))) return rc;
+    if ((rc = run_evaluation(*c, prec, nullptr))) return rc;
+    std::vector<double> red(10 * (size_t)nstruct);
+    GG_CUDA(cudaMemcpyAsync(red.data(), c->out_e.p, sizeof(double) * red.size(), cudaMemcpyDeviceToHost, c->stream));
+    if (forces && n > 0)
+        GG_CUDA(cudaMemcpyAsync(forces, c->out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    GG_CUDA(cudaStreamSynchronize(c->stream));
+    if ((rc = check_device_flags(*c))) return rc;
+    for (int s = 0; s < nstruct; ++s) {
+        if (energies) energies[s] = red[10 * (size_t)s];
+        if (virials) std::memcpy(virials + 9 * (size_t)s, &red[10 * (size_t)s + 1], 9 * sizeof(double));
+    }
     return GAPGPU_OK;
 }
 
@@ -336,6 +556,7 @@ int gapgpu_neighbours(gapgpu_context* c, int n, const double* pos, const double*
     if ((rc = c->pos.ensure(sizeof(double) * 3 * n))) return rc;
     GG_CUDA(cudaMemcpyAsync(c->pos.p, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
     if ((rc = build_neighbours(*c, n, c->pos.as<double>(), lattice, pbc, cutoff, nullptr))) return rc;
+    c->n_total = -1;  // the kept list is not an evaluation's list any more
     if (total) *total = c->n_pairs;
     if (offsets) GG_CUDA(cudaMemcpyAsync(offsets, c->nbr_off.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
     if (capacity >= c->n_pairs && c->n_pairs > 0) {
@@ -364,11 +585,12 @@ int gapgpu_descriptors(gapgpu_context* c, int coordinate, int n, const double* p
     const Coordinate& co = m.coords[coordinate];
     if (co.type != DESC_SOAP) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "gapgpu_descriptors: coordinate is not SOAP");
     int rc;
-    if ((rc = c->pos.ensure(sizeof(double) * 3 * n)) || (rc = c->Z.ensure(sizeof(int) * n))) return rc;
-    GG_CUDA(cudaMemcpyAsync(c->pos.p, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
-    GG_CUDA(cudaMemcpyAsync(c->Z.p, Z, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = copy_inputs(*c, n, pos, Z, nullptr, cudaMemcpyHostToDevice))) return rc;
     if ((rc = build_neighbours(*c, n, c->pos.as<double>(), lattice, pbc, co.cutoff(), nullptr))) return rc;
+    c->n_total = -1;  // the kept list is not an evaluation's list any more
     int nc = 0;
+    if ((rc = c->centres.ensure(sizeof(int) * n))) return rc;
+    c->cur_centres = c->centres.as<int>();
     if ((rc = select_centres(*c, co, n, nullptr, &nc))) return rc;
     if ((rc = soap_forward(*c, co, n, nc))) return rc;
     if (n_centres) *n_centres = nc;
@@ -391,7 +613,10 @@ int gapgpu_descriptors(gapgpu_context* c, int coordinate, int n, const double* p
 
 int gapgpu_context_timings(const gapgpu_context* c, double* ms, int capacity) {
     if (!c || !ms) return 0;
-    double v[7] = {c->t.neighbours, c->t.soap_fwd, c->t.gemm, c->t.soap_bwd, c->t.pair2b, c->t.reduce, c->t.total};
+    gapgpu_context& cc = const_cast<gapgpu_context&>(*c);
+    compute_timings(cc);
+    const Timings& t = cc.t;
+    double v[7] = {t.neighbours, t.soap_fwd, t.gemm, t.soap_bwd, t.pair2b, t.reduce, t.total};
     int k = std::min(capacity, 7);
     for (int i = 0; i < k; ++i) ms[i] = v[i];
     return k;

@@ -22,6 +22,20 @@ struct CellGeom {
     int ncell;
 };
 
+// Geometry record of one structure for the neighbour kernels (connection_calc_connect
+// set-up: effective lattice, cell grid, image ranges, FP32 pre-filter constants).
+struct GeomDev {
+    double lat[9], lat_eff_inv[9], lat_off[3], cutoff;
+    double origin[3];     // Cartesian corner of the effective cell (non-periodic axes)
+    double ginv[9];       // inverse of the true lattice
+    float lat32[9];
+    float lim2;           // (cutoff + margin)^2: FP32 distances above it are certainly outside
+    float sure2;          // (cutoff - margin)^2: FP32 distances below it are certainly inside
+    int cellsN[3], img[3], pbc[3];
+    int cell_base;        // first global cell index of this structure
+    int atom_begin, atom_end;
+};
+
 struct Timings { float neighbours = 0, soap_fwd = 0, gemm = 0, soap_bwd = 0, pair2b = 0, reduce = 0, total = 0; };
 
 }  // namespace gapgpu
@@ -35,17 +49,42 @@ struct gapgpu_context {
     gapgpu::DBuf pos, Z, mask, out_e, out_f, out_v, out_le, out_lv;
     // cells and neighbours
     gapgpu::DBuf cell_key, cell_key2, atom_idx, atom_idx2, cell_start, cell_end, ms, cub_tmp, minmax;
-    gapgpu::DBuf nbr_cnt, nbr_off, nbr_j, nbr_d, nbr_s, nbr_rev, nbr_i, wpos, total;
+    gapgpu::DBuf nbr_cnt, nbr_off, nbr_j, nbr_d, nbr_s, nbr_rev, nbr_i, wpos, total, geoms, sid, dispmax;
+    std::vector<gapgpu::GeomDev> h_geoms;  // geometry of the structures of the last neighbour build
+    int n_atoms_built = 0;
     // per pair / per atom accumulators
     gapgpu::DBuf fpair, epair, eatom, redpart;
     // SOAP / GP workspace
     gapgpu::DBuf flags, centres, ncent, coef, qbuf, qlo, pnorm, Kbuf, Wbuf, Wlo, epart, ecent, Gbuf, scratch;
+    int* cur_centres = nullptr;               // centre list of the coordinate being evaluated
+    std::vector<int> nc_coord;                // centres per coordinate (prepare phase)
+    gapgpu::DBuf chunks, schunk;              // segmented-reduction tables (per batch)
+    std::vector<int> h_chunks, h_schunk;
+    int nstruct = 0, n_total = 0;
+    // CUDA graph of the evaluation phase, keyed by shapes and buffer addresses
+    cudaGraphExec_t graph = nullptr;
+    std::vector<uintptr_t> graph_key, last_key;
+    int graph_mode = 0;                       // 0: never, 1: capture on the second identical call
+    long long graph_hits = 0, graph_launches = 0;
+    // stage timing (CUDA events): neighbour build, then the evaluation's stage boundaries
+    bool timed = true, stage_valid = false, nbr_timed = false;
+    cudaEvent_t nev[2] = {};
+    cudaEvent_t cev[64] = {};
+    int ncev = 0;
     // last results
     long long n_pairs = 0;
     long long launches = 0;
     gapgpu::Timings t;
-    cudaEvent_t ev[8] = {};
-    bool events = false;
+    std::vector<gapgpu::DBuf*> buffers() {
+        return {&pos, &Z, &mask, &out_e, &out_f, &out_v, &out_le, &out_lv, &cell_key, &cell_key2, &atom_idx, &atom_idx2,
+                &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev,
+                &nbr_i, &wpos, &total, &geoms, &sid, &dispmax, &fpair, &epair, &eatom, &redpart, &flags, &centres,
+                &ncent, &coef, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf, &Wlo, &epart, &ecent, &Gbuf, &scratch, &chunks, &schunk};
+    }
+    std::vector<const gapgpu::DBuf*> buffers() const {
+        std::vector<gapgpu::DBuf*> b = const_cast<gapgpu_context*>(this)->buffers();
+        return std::vector<const gapgpu::DBuf*>(b.begin(), b.end());
+    }
     ~gapgpu_context();
 };
 
@@ -53,6 +92,15 @@ namespace gapgpu {
 // neighbours.cu
 int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double* lattice, const int* pbc, double cutoff,
                      const int* d_Z_for_check);
+int build_neighbours_batch(gapgpu_context& c, int nstruct, const int* n_atoms, const double* d_pos, const double* lattices,
+                           const int* pbcs, double cutoff);
+int refresh_distances(gapgpu_context& c, const double* d_pos);
+int max_displacement(gapgpu_context& c, const double* d_pos, const double* d_ref, int n, double* out);
+// calc.cu
+int prepare(gapgpu_context& c, int nstruct, const int* n_atoms, const double* lattices, const int* pbcs, const int* d_mask,
+            double cutoff, bool rebuild);
+int run_evaluation(gapgpu_context& c, int precision, const int* d_mask);
+int check_device_flags(gapgpu_context& c);
 // soap.cu
 int soap_forward(gapgpu_context& c, const Coordinate& co, int n, int nc);
 int soap_backward(gapgpu_context& c, const Coordinate& co, int n, int nc);

@@ -158,7 +158,7 @@ int gp_fp64(gapgpu_context& c, const Coordinate& co, int nc) {
     dim3 g1(ntiles, (nc + BM - 1) / BM);
     k_gemm_nt_epi<<<g1, TPB, 0, c.stream>>>(nc, M, co.soap.dim(), c.qbuf.as<double>(), Dp, co.dX64, Dp, co.dcoef, z, iz,
                                             c.Wbuf.as<double>(), Mp, c.epart.as<double>(), ntiles);
-    k_rowsum_scatter<<<(nc + 127) / 128, 128, 0, c.stream>>>(nc, ntiles, c.epart.as<double>(), c.centres.as<int>(),
+    k_rowsum_scatter<<<(nc + 127) / 128, 128, 0, c.stream>>>(nc, ntiles, c.epart.as<double>(), c.cur_centres,
                                                             c.ecent.as<double>(), c.eatom.as<double>());
     dim3 g2((Dp + BN - 1) / BN, (nc + BM - 1) / BM);
     k_gemm_nn<<<g2, TPB, 0, c.stream>>>(nc, Dp, M, c.Wbuf.as<double>(), Mp, co.dX64, Dp, c.Gbuf.as<double>(), Dp);

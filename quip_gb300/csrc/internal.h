@@ -94,6 +94,7 @@ struct gapgpu_model {
     std::string label;
     int xml_version = 0;
     int device = 0;
+    double* de0 = nullptr;  // e0 per Z on the device
 };
 
 namespace gapgpu {

@@ -17,6 +17,15 @@
 // image cells and emits its full list directly (no atomics: count, scan, fill).
 // Atoms are sorted by cell with a stable radix sort so that each list has a fixed,
 // reproducible order (cell-image loop order, then atom index).
+//
+// Batches: many independent structures are built in one pass.  Each structure has its
+// own geometry record (lattice, cell grid, image ranges) and a block of global cell
+// indices, so atoms of different structures never share a cell and one sort and one
+// pair pass serve the whole batch.  A single structure is a batch of one.
+//
+// Skin reuse (Connection.f95:1086-1125, :1321-1445): a list built at cutoff + skin is
+// kept while every atom has moved less than skin/2 since the build; only the pair
+// displacements are recomputed (k_distances, the same formula as the fill pass).
 #include <cub/cub.cuh>
 #include <cmath>
 #include <cstring>
@@ -33,19 +42,29 @@ __device__ __forceinline__ int pack_shift(int a, int b, int c) {
     return ((a + 512) & 1023) | (((b + 512) & 1023) << 10) | (((c + 512) & 1023) << 20);
 }
 
-struct GeomDev {
-    double lat[9], lat_eff_inv[9], lat_off[3], cutoff;
-    double origin[3];     // Cartesian corner of the effective cell (non-periodic axes)
-    float lat32[9];
-    float lim2;           // (cutoff + margin)^2: FP32 distances above it are certainly outside
-    float sure2;          // (cutoff - margin)^2: FP32 distances below it are certainly inside
-    int cellsN[3], img[3], pbc[3];
-};
+__device__ __forceinline__ int sid_of(const int* __restrict__ sid, int a) { return sid ? sid[a] : 0; }
 
-__global__ void k_assign(int n, const double* __restrict__ pos, GeomDev g, int* __restrict__ key, int* __restrict__ idx,
-                         int* __restrict__ ms, int* __restrict__ bad) {
+// pair displacement d = pos_b - pos_a + L shift, FP64 without fused multiply-add
+// (the order of test_form_bond), and r = |d|.
+__device__ __forceinline__ void pair_vector(const double* __restrict__ pos, const double* lat, int a, int b, int s0, int s1,
+                                            int s2, double& d0, double& d1, double& d2, double& r) {
+    d0 = __dsub_rn(pos[3 * b], pos[3 * a]); d1 = __dsub_rn(pos[3 * b + 1], pos[3 * a + 1]);
+    d2 = __dsub_rn(pos[3 * b + 2], pos[3 * a + 2]);
+    d0 = __dadd_rn(d0, __dmul_rn(lat[0], (double)s0)); d1 = __dadd_rn(d1, __dmul_rn(lat[1], (double)s0));
+    d2 = __dadd_rn(d2, __dmul_rn(lat[2], (double)s0));
+    d0 = __dadd_rn(d0, __dmul_rn(lat[3], (double)s1)); d1 = __dadd_rn(d1, __dmul_rn(lat[4], (double)s1));
+    d2 = __dadd_rn(d2, __dmul_rn(lat[5], (double)s1));
+    d0 = __dadd_rn(d0, __dmul_rn(lat[6], (double)s2)); d1 = __dadd_rn(d1, __dmul_rn(lat[7], (double)s2));
+    d2 = __dadd_rn(d2, __dmul_rn(lat[8], (double)s2));
+    r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+}
+
+__global__ void k_assign(int n, const double* __restrict__ pos, const GeomDev* __restrict__ geoms,
+                         const int* __restrict__ sid, int* __restrict__ key, int* __restrict__ idx, int* __restrict__ ms,
+                         int* __restrict__ bad) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n) return;
+    const GeomDev& g = geoms[sid_of(sid, a)];
     double p[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
     if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) atomicOr(bad, 1);
     int c3[3];
@@ -58,17 +77,19 @@ __global__ void k_assign(int n, const double* __restrict__ pos, GeomDev g, int* 
         ci = ci < 1 ? 1 : (ci > g.cellsN[d] ? g.cellsN[d] : ci);
         c3[d] = ci - 1;
     }
-    key[a] = c3[0] + g.cellsN[0] * (c3[1] + g.cellsN[1] * c3[2]);
+    key[a] = g.cell_base + c3[0] + g.cellsN[0] * (c3[1] + g.cellsN[1] * c3[2]);
     idx[a] = a;
 }
 
 // Wrapped positions (pos + L map_shift - origin) in FP32, in cell-sorted order, for the
 // pre-filter: magnitudes stay within the cell, so FP32 rounding is ~1e-7 of the cell size.
-__global__ void k_wrapped(int n, const double* __restrict__ pos, GeomDev g, const int* __restrict__ sorted,
-                          const int* __restrict__ ms, float4* __restrict__ wpos) {
+__global__ void k_wrapped(int n, const double* __restrict__ pos, const GeomDev* __restrict__ geoms,
+                          const int* __restrict__ sid, const int* __restrict__ sorted, const int* __restrict__ ms,
+                          float4* __restrict__ wpos) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int a = sorted[k];
+    const GeomDev& g = geoms[sid_of(sid, a)];
     double p[3];
     for (int d = 0; d < 3; ++d)
         p[d] = pos[3 * a + d] + g.lat[d] * ms[3 * a] + g.lat[3 + d] * ms[3 * a + 1] + g.lat[6 + d] * ms[3 * a + 2] - g.origin[d];
@@ -96,7 +117,8 @@ __global__ void k_cell_ranges(int n, const int* __restrict__ key, int* __restric
 // into caller-owned arrays, the layout of gapgpu_neighbours; nd/ni are not written.
 template <bool FILL, bool CALLER_LAYOUT = false>
 __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__ pos, const float4* __restrict__ wpos,
-                                               GeomDev g, const int* __restrict__ key_of_atom, const int* __restrict__ ms,
+                                               const GeomDev* __restrict__ geoms, const int* __restrict__ sid,
+                                               const int* __restrict__ key_of_atom, const int* __restrict__ ms,
                                                const int* __restrict__ sorted, const int* __restrict__ cstart,
                                                const int* __restrict__ cend, int* __restrict__ cnt,
                                                const int* __restrict__ off, int* __restrict__ nj, double4* __restrict__ nd,
@@ -105,8 +127,9 @@ __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__
     const int lane = threadIdx.x & 31;
     if (warp >= n) return;
     const int a = sorted[warp];
+    const GeomDev& g = geoms[sid_of(sid, a)];
     const float4 pa32 = wpos[warp];
-    const int lin = key_of_atom[a];
+    const int lin = key_of_atom[a] - g.cell_base;
     int cc[3] = {lin % g.cellsN[0], (lin / g.cellsN[0]) % g.cellsN[1], lin / (g.cellsN[0] * g.cellsN[1])};
     int mn[3], mx[3];
     for (int d = 0; d < 3; ++d) {
@@ -117,8 +140,9 @@ __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__
             mx[d] = (g.img[d] < g.cellsN[d] - c1) ? g.img[d] : g.cellsN[d] - c1;
         }
     }
-    const double pa0 = pos[3 * a], pa1 = pos[3 * a + 1], pa2 = pos[3 * a + 2];
     const int msa0 = ms[3 * a], msa1 = ms[3 * a + 1], msa2 = ms[3 * a + 2];
+    const float lim2 = g.lim2, sure2 = g.sure2;
+    const double cutoff = g.cutoff;
     int count = 0;
     const int base = FILL ? off[a] : 0;
     const unsigned lt = (1u << lane) - 1u;
@@ -134,8 +158,9 @@ __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__
                 int v = cc[0] + i2;
                 int i3 = g.cellsN[0] > 1 ? ((v % g.cellsN[0]) + g.cellsN[0]) % g.cellsN[0] : 0;
                 int i4 = (v - i3) / g.cellsN[0];
-                const int cl = i3 + g.cellsN[0] * (j3 + g.cellsN[1] * k3);
-                const bool same_cell = (cl == lin);
+                const int cl_loc = i3 + g.cellsN[0] * (j3 + g.cellsN[1] * k3);
+                const int cl = g.cell_base + cl_loc;
+                const bool same_cell = (cl_loc == lin);
                 const float ox = g.lat32[0] * i4 + g.lat32[3] * j4 + g.lat32[6] * k4 - pa32.x;
                 const float oy = g.lat32[1] * i4 + g.lat32[4] * j4 + g.lat32[7] * k4 - pa32.y;
                 const float oz = g.lat32[2] * i4 + g.lat32[5] * j4 + g.lat32[8] * k4 - pa32.z;
@@ -151,24 +176,12 @@ __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__
                         float fx = pb.x + ox, fy = pb.y + oy, fz = pb.z + oz;
                         const bool self0 = (b == a && i4 == 0 && j4 == 0 && k4 == 0 && same_cell);
                         const float r2 = fx * fx + fy * fy + fz * fz;
-                        const bool sure = r2 < g.sure2;
+                        const bool sure = r2 < sure2;
                         if (!FILL && sure && !self0) keep = true;
-                        else if (!self0 && r2 < g.lim2) {
+                        else if (!self0 && r2 < lim2) {
                             s0 = i4 - msa0 + ms[3 * b]; s1 = j4 - msa1 + ms[3 * b + 1]; s2 = k4 - msa2 + ms[3 * b + 2];
-                            d0 = __dsub_rn(pos[3 * b], pa0); d1 = __dsub_rn(pos[3 * b + 1], pa1); d2 = __dsub_rn(pos[3 * b + 2], pa2);
-                            d0 = __dadd_rn(d0, __dmul_rn(g.lat[0], (double)s0)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[1], (double)s0));
-                            d2 = __dadd_rn(d2, __dmul_rn(g.lat[2], (double)s0));
-                            d0 = __dadd_rn(d0, __dmul_rn(g.lat[3], (double)s1)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[4], (double)s1));
-                            d2 = __dadd_rn(d2, __dmul_rn(g.lat[5], (double)s1));
-                            d0 = __dadd_rn(d0, __dmul_rn(g.lat[6], (double)s2)); d1 = __dadd_rn(d1, __dmul_rn(g.lat[7], (double)s2));
-                            d2 = __dadd_rn(d2, __dmul_rn(g.lat[8], (double)s2));
-                            if (sure) {
-                                r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
-                                keep = true;
-                            } else if (!(d0 > g.cutoff || d1 > g.cutoff || d2 > g.cutoff)) {
-                                r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
-                                keep = r < g.cutoff;
-                            }
+                            pair_vector(pos, g.lat, a, b, s0, s1, s2, d0, d1, d2, r);
+                            keep = sure || (!(d0 > cutoff || d1 > cutoff || d2 > cutoff) && r < cutoff);
                         }
                     }
                     const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -208,6 +221,79 @@ __global__ void k_reverse(long long P, const int* __restrict__ off, const int* _
     if (found < 0) atomicOr(bad, 4);
 }
 
+// connection_calc_dists: new displacements for an existing list (same formula as the
+// fill pass, so a refreshed list equals a rebuilt one entry for entry).
+__global__ void k_distances(long long P, const double* __restrict__ pos, const GeomDev* __restrict__ geoms,
+                            const int* __restrict__ sid, const int* __restrict__ ni, const int* __restrict__ nj,
+                            const int* __restrict__ ns, double4* __restrict__ nd, int* __restrict__ bad) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int a = ni[p], b = nj[p], s = ns[p];
+    const GeomDev& g = geoms[sid_of(sid, a)];
+    double d0, d1, d2, r;
+    pair_vector(pos, g.lat, a, b, (s & 1023) - 512, ((s >> 10) & 1023) - 512, ((s >> 20) & 1023) - 512, d0, d1, d2, r);
+    nd[p] = make_double4(d0, d1, d2, r);
+    if (r < 1e-10) atomicOr(bad, 2);
+}
+
+// Largest displacement since the list was built, minimum image on periodic axes
+// (distance_min_image of Connection.f95:1108).  Non-negative doubles order like their
+// bit patterns, so the maximum is an integer atomicMax.
+__global__ void k_max_disp(int n, const double* __restrict__ pos, const double* __restrict__ ref,
+                           const GeomDev* __restrict__ geoms, const int* __restrict__ sid,
+                           unsigned long long* __restrict__ out) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double dmax = 0.0;
+    if (a < n) {
+        const GeomDev& g = geoms[sid_of(sid, a)];
+        double dp[3] = {pos[3 * a] - ref[3 * a], pos[3 * a + 1] - ref[3 * a + 1], pos[3 * a + 2] - ref[3 * a + 2]};
+        double f[3];
+        for (int d = 0; d < 3; ++d) {
+            f[d] = g.ginv[d] * dp[0] + g.ginv[3 + d] * dp[1] + g.ginv[6 + d] * dp[2];
+            if (g.pbc[d]) f[d] -= rint(f[d]);
+        }
+        double c2 = 0;
+        for (int d = 0; d < 3; ++d) {
+            double x = g.lat[d] * f[0] + g.lat[3 + d] * f[1] + g.lat[6 + d] * f[2];
+            c2 += x * x;
+        }
+        dmax = sqrt(c2);
+    }
+    for (int o = 16; o > 0; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(dmax));
+}
+
+// Per-structure extent in fractional coordinates of the true lattice (calc_lat_eff):
+// one block per structure.
+__global__ void k_latpos_minmax(const double* __restrict__ pos, const GeomDev* __restrict__ geoms, double* __restrict__ out) {
+    __shared__ double smn[3][256], smx[3][256];
+    const GeomDev& g = geoms[blockIdx.x];
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int a = g.atom_begin + threadIdx.x; a < g.atom_end; a += blockDim.x) {
+        for (int d = 0; d < 3; ++d) {
+            double lp = g.ginv[d] * pos[3 * a] + g.ginv[3 + d] * pos[3 * a + 1] + g.ginv[6 + d] * pos[3 * a + 2];
+            mn[d] = fmin(mn[d], lp); mx[d] = fmax(mx[d], lp);
+        }
+    }
+    for (int d = 0; d < 3; ++d) { smn[d][threadIdx.x] = mn[d]; smx[d][threadIdx.x] = mx[d]; }
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int d = 0; d < 3; ++d) {
+                smn[d][threadIdx.x] = fmin(smn[d][threadIdx.x], smn[d][threadIdx.x + s]);
+                smx[d][threadIdx.x] = fmax(smx[d][threadIdx.x], smx[d][threadIdx.x + s]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; ++d) { out[6 * blockIdx.x + d] = smn[d][0]; out[6 * blockIdx.x + 3 + d] = smx[d][0]; }
+}
+
+__global__ void k_fill_sid(const GeomDev* __restrict__ geoms, int* __restrict__ sid) {
+    const GeomDev& g = geoms[blockIdx.x];
+    for (int a = g.atom_begin + threadIdx.x; a < g.atom_end; a += blockDim.x) sid[a] = blockIdx.x;
+}
+
 void inv3(const double* a, double* g) {
     auto A = [&](int r, int c) { return a[3 * c + r]; };
     double det = A(0, 0) * (A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) - A(0, 1) * (A(1, 0) * A(2, 2) - A(1, 2) * A(2, 0)) +
@@ -227,71 +313,29 @@ void cross3(const double* a, const double* b, double* c) {
     c[0] = a[1] * b[2] - a[2] * b[1]; c[1] = a[2] * b[0] - a[0] * b[2]; c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-__global__ void k_latpos_minmax(int n, const double* __restrict__ pos, GeomDev g, double* __restrict__ out) {
-    // one block: min/max of fractional coordinates per axis (calc_lat_eff)
-    __shared__ double smn[3][256], smx[3][256];
-    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
-    for (int a = threadIdx.x; a < n; a += blockDim.x) {
-        for (int d = 0; d < 3; ++d) {
-            double lp = g.lat_eff_inv[d] * pos[3 * a] + g.lat_eff_inv[3 + d] * pos[3 * a + 1] + g.lat_eff_inv[6 + d] * pos[3 * a + 2];
-            mn[d] = fmin(mn[d], lp); mx[d] = fmax(mx[d], lp);
-        }
-    }
-    for (int d = 0; d < 3; ++d) { smn[d][threadIdx.x] = mn[d]; smx[d][threadIdx.x] = mx[d]; }
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s)
-            for (int d = 0; d < 3; ++d) {
-                smn[d][threadIdx.x] = fmin(smn[d][threadIdx.x], smn[d][threadIdx.x + s]);
-                smx[d][threadIdx.x] = fmax(smx[d][threadIdx.x], smx[d][threadIdx.x + s]);
-            }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0)
-        for (int d = 0; d < 3; ++d) { out[d] = smn[d][0]; out[3 + d] = smx[d][0]; }
-}
-
-}  // namespace
-
-int DBuf::ensure(size_t bytes) {
-    if (bytes <= cap && p) return GAPGPU_OK;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t want = std::max<size_t>(bytes + bytes / 4, 256);
-    GG_CUDA(cudaMalloc(&p, want));
-    cap = want;
-    return GAPGPU_OK;
-}
-void DBuf::release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-}
-
-// Host set-up of connection_calc_connect for one call: effective lattice of clusters
-// and mixed boundary conditions (calc_lat_eff), cell grid (divide_cell), image ranges
-// (fit_box_in_cell) and the FP32 pre-filter constants.  d_minmax is 6 doubles of device
-// scratch, used only when an axis is not periodic.
-static int neighbour_geometry(int n, const double* d_pos, const double* lattice, const int* pbc, double cutoff, double* d_minmax,
-                       cudaStream_t st, GeomDev& g, long long& launches) {
+// First half of the host set-up of connection_calc_connect: lattice, its inverse,
+// boundary conditions.
+int geom_begin(const double* lattice, const int* pbc, double cutoff, GeomDev& g) {
     if (!(cutoff >= 0.0)) GG_FAIL(GAPGPU_ERR_ATOMS, "calc_connect: negative cutoff radius");
     std::memset(&g, 0, sizeof g);
     std::memcpy(g.lat, lattice, sizeof g.lat);
     g.cutoff = cutoff;
     for (int d = 0; d < 3; ++d) g.pbc[d] = pbc[d] ? 1 : 0;
-    double gi[9];
-    inv3(lattice, gi);
-    for (double v : gi) if (!std::isfinite(v)) GG_FAIL(GAPGPU_ERR_ATOMS, "lattice is singular");
+    inv3(lattice, g.ginv);
+    for (double v : g.ginv) if (!std::isfinite(v)) GG_FAIL(GAPGPU_ERR_ATOMS, "lattice is singular");
+    std::memcpy(g.lat_eff_inv, g.ginv, sizeof g.ginv);
+    return GAPGPU_OK;
+}
+
+// Second half: effective lattice of clusters and mixed boundary conditions
+// (calc_lat_eff, Connection.f95:740-763, from the fractional extent mm of the atoms),
+// cell grid (divide_cell), image ranges (fit_box_in_cell) and the FP32 pre-filter.
+int geom_finish(GeomDev& g, int n, const double* mm) {
+    const double* lattice = g.lat;
+    const double cutoff = g.cutoff;
     double lat_eff[9];
     std::memcpy(lat_eff, lattice, sizeof lat_eff);
-    std::memcpy(g.lat_eff_inv, gi, sizeof gi);
-    if (!g.pbc[0] || !g.pbc[1] || !g.pbc[2]) {  // calc_lat_eff (Connection.f95:740-763)
-        k_latpos_minmax<<<1, 256, 0, st>>>(n, d_pos, g, d_minmax);
-        launches++;
-        double mm[6];
-        GG_CUDA(cudaMemcpyAsync(mm, d_minmax, sizeof mm, cudaMemcpyDeviceToHost, st));
-        GG_CUDA(cudaStreamSynchronize(st));
+    if (mm) {
         for (int d = 0; d < 3; ++d) {
             if (g.pbc[d]) continue;
             if (mm[d] <= 0.5 || mm[3 + d] >= 0.5) {
@@ -329,7 +373,8 @@ static int neighbour_geometry(int n, const double* d_pos, const double* lattice,
             for (int j = -1; j <= 1; j += 2)
                 for (int i = -1; i <= 1; i += 2) {
                     double v[3] = {i * cutoff, j * cutoff, k * cutoff};
-                    for (int d = 0; d < 3; ++d) mx[d] = std::max(mx[d], std::fabs(gi[d] * v[0] + gi[3 + d] * v[1] + gi[6 + d] * v[2]));
+                    for (int d = 0; d < 3; ++d)
+                        mx[d] = std::max(mx[d], std::fabs(g.ginv[d] * v[0] + g.ginv[3 + d] * v[1] + g.ginv[6 + d] * v[2]));
                 }
         for (int d = 0; d < 3; ++d) {
             int nn = (int)std::ceil(2.0 * mx[d]);
@@ -353,15 +398,76 @@ static int neighbour_geometry(int n, const double* d_pos, const double* lattice,
     return GAPGPU_OK;
 }
 
-int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double* lattice, const int* pbc, double cutoff,
-                     const int*) {
+bool any_open(const GeomDev& g) { return !g.pbc[0] || !g.pbc[1] || !g.pbc[2]; }
+
+}  // namespace
+
+int DBuf::ensure(size_t bytes) {
+    if (bytes <= cap && p) return GAPGPU_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+    GG_CUDA(cudaMalloc(&p, want));
+    cap = want;
+    return GAPGPU_OK;
+}
+void DBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+}
+
+int build_neighbours_batch(gapgpu_context& c, int nstruct, const int* n_atoms, const double* d_pos, const double* lattices,
+                           const int* pbcs, double cutoff) {
     cudaStream_t st = c.stream;
-    GeomDev g;
-    int rc;
-    if ((rc = c.minmax.ensure(6 * sizeof(double))) ||
-        (rc = neighbour_geometry(n, d_pos, lattice, pbc, cutoff, c.minmax.as<double>(), st, g, c.launches)))
-        return rc;
-    const int ncell = g.cellsN[0] * g.cellsN[1] * g.cellsN[2];
+    if (nstruct < 1) GG_FAIL(GAPGPU_ERR_ARG, "neighbour build: no structures");
+    std::vector<GeomDev>& hg = c.h_geoms;
+    hg.assign(nstruct, GeomDev{});
+    int n = 0, rc;
+    bool open = false;
+    for (int s = 0; s < nstruct; ++s) {
+        if (n_atoms[s] < 0) GG_FAIL(GAPGPU_ERR_ARG, "negative atom count");
+        if ((rc = geom_begin(lattices + 9 * s, pbcs + 3 * s, cutoff, hg[s]))) return rc;
+        hg[s].atom_begin = n;
+        n += n_atoms[s];
+        hg[s].atom_end = n;
+        open = open || any_open(hg[s]);
+    }
+    if ((rc = c.geoms.ensure(sizeof(GeomDev) * nstruct))) return rc;
+    const int* sid = nullptr;
+    if (nstruct > 1) {
+        if ((rc = c.sid.ensure(sizeof(int) * std::max(n, 1)))) return rc;
+        sid = c.sid.as<int>();
+    }
+    std::vector<double> mm;
+    if (open || nstruct > 1) {
+        GG_CUDA(cudaMemcpyAsync(c.geoms.p, hg.data(), sizeof(GeomDev) * nstruct, cudaMemcpyHostToDevice, st));
+        if (nstruct > 1) {
+            k_fill_sid<<<nstruct, 128, 0, st>>>(c.geoms.as<GeomDev>(), c.sid.as<int>());
+            c.launches++;
+        }
+        if (open) {
+            if ((rc = c.minmax.ensure(6 * sizeof(double) * nstruct))) return rc;
+            k_latpos_minmax<<<nstruct, 256, 0, st>>>(d_pos, c.geoms.as<GeomDev>(), c.minmax.as<double>());
+            c.launches++;
+            mm.resize(6 * (size_t)nstruct);
+            GG_CUDA(cudaMemcpyAsync(mm.data(), c.minmax.p, sizeof(double) * mm.size(), cudaMemcpyDeviceToHost, st));
+        }
+        GG_CUDA(cudaStreamSynchronize(st));
+    }
+    long long ncell = 0;
+    for (int s = 0; s < nstruct; ++s) {
+        if ((rc = geom_finish(hg[s], n_atoms[s], any_open(hg[s]) ? &mm[6 * (size_t)s] : nullptr))) return rc;
+        hg[s].cell_base = (int)ncell;
+        ncell += (long long)hg[s].cellsN[0] * hg[s].cellsN[1] * hg[s].cellsN[2];
+    }
+    if (ncell > (1LL << 30)) GG_FAIL(GAPGPU_ERR_ATOMS, "calc_connect: too many cells");
+    GG_CUDA(cudaMemcpyAsync(c.geoms.p, hg.data(), sizeof(GeomDev) * nstruct, cudaMemcpyHostToDevice, st));
+    c.n_atoms_built = n;
+    c.n_pairs = 0;
+    if (n == 0) return GAPGPU_OK;
+    const GeomDev* dg = c.geoms.as<GeomDev>();
     if ((rc = c.cell_key.ensure(sizeof(int) * n)) || (rc = c.cell_key2.ensure(sizeof(int) * n)) ||
         (rc = c.atom_idx.ensure(sizeof(int) * n)) || (rc = c.atom_idx2.ensure(sizeof(int) * n)) ||
         (rc = c.ms.ensure(sizeof(int) * 3 * n)) || (rc = c.cell_start.ensure(sizeof(int) * ncell)) ||
@@ -373,10 +479,10 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
     GG_CUDA(cudaMemsetAsync(c.total.p, 0, sizeof(int) * 4, st));
     const int TB = 128, nb = (n + TB - 1) / TB;
     const int nbw = (int)(((long long)n * 32 + TB - 1) / TB);  // one warp per atom
-    k_assign<<<nb, TB, 0, st>>>(n, d_pos, g, c.cell_key.as<int>(), c.atom_idx.as<int>(), c.ms.as<int>(), bad);
+    k_assign<<<nb, TB, 0, st>>>(n, d_pos, dg, sid, c.cell_key.as<int>(), c.atom_idx.as<int>(), c.ms.as<int>(), bad);
     // stable sort atoms by cell
     int endbit = 1;
-    while ((1 << endbit) < ncell && endbit < 31) ++endbit;
+    while ((1LL << endbit) < ncell && endbit < 31) ++endbit;
     size_t tmp = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, tmp, c.cell_key.as<int>(), c.cell_key2.as<int>(), c.atom_idx.as<int>(),
                                     c.atom_idx2.as<int>(), n, 0, endbit, st);
@@ -388,8 +494,8 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
     GG_CUDA(cudaMemsetAsync(c.cell_start.p, 0, sizeof(int) * ncell, st));
     GG_CUDA(cudaMemsetAsync(c.cell_end.p, 0, sizeof(int) * ncell, st));
     k_cell_ranges<<<nb, TB, 0, st>>>(n, c.cell_key2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>());
-    k_wrapped<<<nb, TB, 0, st>>>(n, d_pos, g, c.atom_idx2.as<int>(), c.ms.as<int>(), c.wpos.as<float4>());
-    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), g, c.cell_key.as<int>(), c.ms.as<int>(),
+    k_wrapped<<<nb, TB, 0, st>>>(n, d_pos, dg, sid, c.atom_idx2.as<int>(), c.ms.as<int>(), c.wpos.as<float4>());
+    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), dg, sid, c.cell_key.as<int>(), c.ms.as<int>(),
                                        c.atom_idx2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>(),
                                        c.nbr_cnt.as<int>(), nullptr, nullptr, nullptr, nullptr, nullptr, bad);
     GG_CUDA(cudaMemsetAsync(c.nbr_cnt.as<int>() + n, 0, sizeof(int), st));
@@ -405,7 +511,7 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
         (rc = c.nbr_s.ensure(sizeof(int) * P)) || (rc = c.nbr_rev.ensure(sizeof(int) * P)) ||
         (rc = c.nbr_i.ensure(sizeof(int) * P)))
         return rc;
-    k_pairs<true><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), g, c.cell_key.as<int>(), c.ms.as<int>(),
+    k_pairs<true><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), dg, sid, c.cell_key.as<int>(), c.ms.as<int>(),
                                       c.atom_idx2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>(), nullptr,
                                       c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.nbr_s.as<int>(),
                                       c.nbr_i.as<int>(), bad);
@@ -423,6 +529,40 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
     return GAPGPU_OK;
 }
 
+int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double* lattice, const int* pbc, double cutoff,
+                     const int*) {
+    return build_neighbours_batch(c, 1, &n, d_pos, lattice, pbc, cutoff);
+}
+
+int refresh_distances(gapgpu_context& c, const double* d_pos) {
+    const long long P = c.n_pairs;
+    if (P == 0) return GAPGPU_OK;
+    int* bad = c.total.as<int>() + 2;
+    k_distances<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(
+        P, d_pos, c.geoms.as<GeomDev>(), c.h_geoms.size() > 1 ? c.sid.as<int>() : nullptr, c.nbr_i.as<int>(),
+        c.nbr_j.as<int>(), c.nbr_s.as<int>(), c.nbr_d.as<double4>(), bad);
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
+int max_displacement(gapgpu_context& c, const double* d_pos, const double* d_ref, int n, double* out) {
+    int rc;
+    if ((rc = c.dispmax.ensure(sizeof(unsigned long long)))) return rc;
+    GG_CUDA(cudaMemsetAsync(c.dispmax.p, 0, sizeof(unsigned long long), c.stream));
+    if (n > 0) {
+        k_max_disp<<<(n + 255) / 256, 256, 0, c.stream>>>(n, d_pos, d_ref, c.geoms.as<GeomDev>(),
+                                                         c.h_geoms.size() > 1 ? c.sid.as<int>() : nullptr,
+                                                         c.dispmax.as<unsigned long long>());
+        c.launches++;
+    }
+    unsigned long long bits = 0;
+    GG_CUDA(cudaMemcpyAsync(&bits, c.dispmax.p, sizeof bits, cudaMemcpyDeviceToHost, c.stream));
+    GG_CUDA(cudaStreamSynchronize(c.stream));
+    std::memcpy(out, &bits, sizeof(double));
+    return GAPGPU_OK;
+}
+
 }  // namespace gapgpu
 
 // ---------------------------------------------------------------------------------
@@ -436,6 +576,7 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
 //   cstart, cend            int[MAX_CELLS]    atom range of each cell
 //   wpos                    float4[MAX]       wrapped FP32 positions in cell order
 //   minmax                  double[6]         fractional extent (non-periodic axes)
+//   geom                    GeomDev           geometry record of the structure
 //   flags                   int[4]            error bits of the kernels
 //   cub                     bytes             temporary storage of the radix sort and the scan
 namespace gapgpu {
@@ -456,7 +597,8 @@ constexpr size_t SO_CSTART = SO_CNT + al256(sizeof(int) * (STATIC_MAX_ATOMS + 1)
 constexpr size_t SO_CEND = SO_CSTART + al256(sizeof(int) * STATIC_MAX_CELLS);
 constexpr size_t SO_WPOS = SO_CEND + al256(sizeof(int) * STATIC_MAX_CELLS);
 constexpr size_t SO_MINMAX = SO_WPOS + al256(sizeof(float4) * STATIC_MAX_ATOMS);
-constexpr size_t SO_FLAGS = SO_MINMAX + al256(sizeof(double) * 6);
+constexpr size_t SO_GEOM = SO_MINMAX + al256(sizeof(double) * 6);
+constexpr size_t SO_FLAGS = SO_GEOM + al256(sizeof(GeomDev));
 constexpr size_t SO_CUB = SO_FLAGS + al256(sizeof(int) * 4);
 constexpr size_t STATIC_SCRATCH_BYTES = SO_CUB + STATIC_CUB_BYTES;
 
@@ -514,10 +656,21 @@ extern "C" int gapgpu_neighbours_static(int n, const double* d_pos, const double
     int* bad = reinterpret_cast<int*>(base + SO_FLAGS);
     void* cub_tmp = base + SO_CUB;
 
+    GeomDev* dg = reinterpret_cast<GeomDev*>(base + SO_GEOM);
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
-    long long launches = 0;
     GeomDev g;
-    if ((rc = neighbour_geometry(n, d_pos, lattice, pbc, cutoff, minmax, st, g, launches))) return rc;
+    if ((rc = geom_begin(lattice, pbc, cutoff, g))) return rc;
+    g.atom_begin = 0;
+    g.atom_end = n;
+    double mm[6];
+    if (any_open(g)) {  // fractional extent of the atoms for calc_lat_eff
+        GG_CUDA(cudaMemcpyAsync(dg, &g, sizeof g, cudaMemcpyHostToDevice, st));
+        k_latpos_minmax<<<1, 256, 0, st>>>(d_pos, dg, minmax);
+        GG_CUDA(cudaMemcpyAsync(mm, minmax, sizeof mm, cudaMemcpyDeviceToHost, st));
+        GG_CUDA(cudaStreamSynchronize(st));
+    }
+    if ((rc = geom_finish(g, n, any_open(g) ? mm : nullptr))) return rc;
+    GG_CUDA(cudaMemcpyAsync(dg, &g, sizeof g, cudaMemcpyHostToDevice, st));
     const int ncell = g.cellsN[0] * g.cellsN[1] * g.cellsN[2];
     if (ncell > STATIC_MAX_CELLS) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_neighbours_static: cell grid above the static limit");
     int endbit = 1;
@@ -534,12 +687,12 @@ extern "C" int gapgpu_neighbours_static(int n, const double* d_pos, const double
     GG_CUDA(cudaMemsetAsync(cnt + n, 0, sizeof(int), st));
     const int TB = 128, nb = (n + TB - 1) / TB;
     const int nbw = (int)(((long long)n * 32 + TB - 1) / TB);
-    k_assign<<<nb, TB, 0, st>>>(n, d_pos, g, key, idx, ms, bad);
+    k_assign<<<nb, TB, 0, st>>>(n, d_pos, dg, nullptr, key, idx, ms, bad);
     GG_CUDA(cub::DeviceRadixSort::SortPairs(cub_tmp, t_sort, key, key2, idx, idx2, n, 0, endbit, st));
     k_cell_ranges<<<nb, TB, 0, st>>>(n, key2, cstart, cend);
-    k_wrapped<<<nb, TB, 0, st>>>(n, d_pos, g, idx2, ms, wpos);
-    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, wpos, g, key, ms, idx2, cstart, cend, cnt, nullptr, nullptr, nullptr,
-                                       nullptr, nullptr, bad);
+    k_wrapped<<<nb, TB, 0, st>>>(n, d_pos, dg, nullptr, idx2, ms, wpos);
+    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, wpos, dg, nullptr, key, ms, idx2, cstart, cend, cnt, nullptr, nullptr,
+                                       nullptr, nullptr, nullptr, bad);
     GG_CUDA(cub::DeviceScan::ExclusiveSum(cub_tmp, t_scan, cnt, d_offsets, n + 1, st));
     int tot = 0;
     GG_CUDA(cudaMemcpyAsync(&tot, d_offsets + n, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -547,8 +700,8 @@ extern "C" int gapgpu_neighbours_static(int n, const double* d_pos, const double
     if (tot < 0) GG_FAIL(GAPGPU_ERR_ATOMS, "neighbour list larger than 2^31 entries");
     *total = tot;
     if (tot > 0 && capacity >= tot && d_nbr_j && d_nbr_shift)
-        k_pairs<true, true><<<nbw, TB, 0, st>>>(n, d_pos, wpos, g, key, ms, idx2, cstart, cend, nullptr, d_offsets, d_nbr_j,
-                                                nullptr, d_nbr_shift, nullptr, bad);
+        k_pairs<true, true><<<nbw, TB, 0, st>>>(n, d_pos, wpos, dg, nullptr, key, ms, idx2, cstart, cend, nullptr, d_offsets,
+                                                d_nbr_j, nullptr, d_nbr_shift, nullptr, bad);
     int flags = 0;
     GG_CUDA(cudaMemcpyAsync(&flags, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     GG_CUDA(cudaStreamSynchronize(st));

@@ -124,10 +124,13 @@ __global__ void k_gather(int n, const int* __restrict__ Z, const int* __restrict
     for (int k = 0; k < 9; ++k) LV[9 * (size_t)a + k] = escale * v[k];
 }
 
-// Deterministic sums E = sum le, virial = sum LV in two fixed-order levels: block b
-// reduces atoms [b*RED_CHUNK, (b+1)*RED_CHUNK) into part[b][10]; one block then sums the
-// partials in block order.  No atomics, so the result is bit-identical run to run.
-constexpr int RED_THREADS = 256, RED_CHUNK = 4096;
+// Deterministic per-structure sums E_s = sum le, virial_s = sum LV in two fixed-order
+// levels: chunk k (atoms chunk[k].x .. chunk[k].y - 1 of one structure, RED_CHUNK at a
+// time from the structure's first atom) is reduced by one block into part[k][10]; then
+// one block per structure sums its chunks in order.  The arithmetic of a structure does
+// not depend on where it sits in a batch, so a structure gives the same bits alone and
+// batched, run after run (no atomics).
+constexpr int RED_THREADS = 256;
 
 __device__ __forceinline__ void block_sum10(double (&acc)[10], double (*sh)[RED_THREADS]) {
     for (int k = 0; k < 10; ++k) sh[k][threadIdx.x] = acc[k];
@@ -139,27 +142,27 @@ __device__ __forceinline__ void block_sum10(double (&acc)[10], double (*sh)[RED_
     }
 }
 
-__global__ void __launch_bounds__(RED_THREADS) k_reduce_part(int n, const double* __restrict__ le,
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_part(const int2* __restrict__ chunk, const double* __restrict__ le,
                                                              const double* __restrict__ LV, double* __restrict__ part) {
     __shared__ double sh[10][RED_THREADS];
     double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const int a0 = blockIdx.x * RED_CHUNK, a1 = min(n, a0 + RED_CHUNK);
-    for (int a = a0 + threadIdx.x; a < a1; a += RED_THREADS) {
+    const int2 ch = chunk[blockIdx.x];
+    for (int a = ch.x + threadIdx.x; a < ch.y; a += RED_THREADS) {
         acc[0] += le[a];
         for (int k = 0; k < 9; ++k) acc[1 + k] += LV[9 * (size_t)a + k];
     }
     block_sum10(acc, sh);
-    if (threadIdx.x < 10) part[10 * blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
+    if (threadIdx.x < 10) part[10 * (size_t)blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-__global__ void __launch_bounds__(RED_THREADS) k_reduce_final(int nparts, const double* __restrict__ part,
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_final(const int* __restrict__ schunk, const double* __restrict__ part,
                                                               double* __restrict__ out) {
     __shared__ double sh[10][RED_THREADS];
     double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int b = threadIdx.x; b < nparts; b += RED_THREADS)
-        for (int k = 0; k < 10; ++k) acc[k] += part[10 * b + k];
+    for (int b = schunk[blockIdx.x] + threadIdx.x; b < schunk[blockIdx.x + 1]; b += RED_THREADS)
+        for (int k = 0; k < 10; ++k) acc[k] += part[10 * (size_t)b + k];
     block_sum10(acc, sh);
-    if (threadIdx.x < 10) out[threadIdx.x] = sh[threadIdx.x][0];
+    if (threadIdx.x < 10) out[10 * (size_t)blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
 }
 
 }  // namespace
@@ -187,22 +190,15 @@ int pair_2b(gapgpu_context& c, const Coordinate& co, int n, const int* d_mask) {
 }
 
 int gather_outputs(gapgpu_context& c, const gapgpu_model& m, int n, const int* d_mask) {
-    int rc;
-    if ((rc = c.out_le.ensure(sizeof(double) * n)) || (rc = c.out_f.ensure(sizeof(double) * 3 * n)) ||
-        (rc = c.out_lv.ensure(sizeof(double) * 9 * n)) || (rc = c.out_e.ensure(sizeof(double) * (10 + 128))))
-        return rc;
-    double* e0 = c.out_e.as<double>() + 10;
-    GG_CUDA(cudaMemcpyAsync(e0, m.e0, sizeof(double) * 128, cudaMemcpyHostToDevice, c.stream));
+    const int nchunks = (int)c.h_chunks.size() / 2, ns = c.nstruct;
     const int TB = 128;
     k_gather<<<(n + TB - 1) / TB, TB, 0, c.stream>>>(n, c.Z.as<int>(), d_mask, c.nbr_off.as<int>(), c.nbr_rev.as<int>(),
                                                     c.nbr_d.as<double4>(), c.fpair.as<double>(), c.epair.as<double>(),
-                                                    c.eatom.as<double>(), e0, m.E_scale, c.out_le.as<double>(),
+                                                    c.eatom.as<double>(), m.de0, m.E_scale, c.out_le.as<double>(),
                                                     c.out_f.as<double>(), c.out_lv.as<double>());
-    const int nparts = (n + RED_CHUNK - 1) / RED_CHUNK;
-    if ((rc = c.redpart.ensure(sizeof(double) * 10 * (size_t)nparts))) return rc;
-    k_reduce_part<<<nparts, RED_THREADS, 0, c.stream>>>(n, c.out_le.as<double>(), c.out_lv.as<double>(),
-                                                       c.redpart.as<double>());
-    k_reduce_final<<<1, RED_THREADS, 0, c.stream>>>(nparts, c.redpart.as<double>(), c.out_e.as<double>());
+    k_reduce_part<<<nchunks, RED_THREADS, 0, c.stream>>>(c.chunks.as<int2>(), c.out_le.as<double>(), c.out_lv.as<double>(),
+                                                        c.redpart.as<double>());
+    k_reduce_final<<<ns, RED_THREADS, 0, c.stream>>>(c.schunk.as<int>(), c.redpart.as<double>(), c.out_e.as<double>());
     c.launches += 3;
     GG_CUDA(cudaGetLastError());
     return GAPGPU_OK;

@@ -623,7 +623,7 @@ int launch_forward(gapgpu_context& c, const Coordinate& co, int nc) {
     if (sm > 200 * 1024) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the shared-memory forward kernel");
     GG_CUDA(cudaFuncSetAttribute(k_soap_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const R* tab = static_cast<const R*>(co.dtab[sizeof(R) == 4 ? 1 : 0]);
-    k_soap_forward<R><<<nc, FWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.centres.as<int>(), c.Z.as<int>(),
+    k_soap_forward<R><<<nc, FWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.cur_centres, c.Z.as<int>(),
                                                          c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(),
                                                          c.scratch.as<R>(), c.qbuf.as<R>(), c.pnorm.as<double>());
     c.launches++;
@@ -638,7 +638,7 @@ int launch_backward(gapgpu_context& c, const Coordinate& co, int nc) {
     if (sm > 200 * 1024) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the shared-memory backward kernel");
     GG_CUDA(cudaFuncSetAttribute(k_soap_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const R* tab = static_cast<const R*>(co.dtab[sizeof(R) == 4 ? 1 : 0]);
-    k_soap_backward<R><<<nc, BWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.centres.as<int>(), c.Z.as<int>(),
+    k_soap_backward<R><<<nc, BWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.cur_centres, c.Z.as<int>(),
                                                           c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(),
                                                           c.scratch.as<R>(), c.qbuf.as<R>(), c.pnorm.as<double>(),
                                                           c.Gbuf.as<R>(), c.fpair.as<double>());
@@ -679,8 +679,8 @@ int upload_soap_tables(Coordinate& co) {
 
 int select_centres(gapgpu_context& c, const Coordinate& co, int n, const int* d_mask, int* nc_out) {
     int rc;
-    if ((rc = c.flags.ensure(sizeof(int) * n)) || (rc = c.centres.ensure(sizeof(int) * n)) ||
-        (rc = c.ncent.ensure(sizeof(int) * 2)) || (rc = c.eatom.ensure(sizeof(double) * n)))
+    if ((rc = c.flags.ensure(sizeof(int) * n)) || (rc = c.ncent.ensure(sizeof(int) * 2)) ||
+        (rc = c.eatom.ensure(sizeof(double) * n)))
         return rc;
     SoapConst sc = soap_const(co);
     int zl[MAX_CENTRE_Z];
@@ -695,10 +695,10 @@ int select_centres(gapgpu_context& c, const Coordinate& co, int n, const int* d_
     k_iota<<<nb, TB, 0, c.stream>>>(n, c.atom_idx.as<int>());
     c.launches += 2;
     size_t tmp = 0;
-    cub::DeviceSelect::Flagged(nullptr, tmp, c.atom_idx.as<int>(), c.flags.as<int>(), c.centres.as<int>(), c.ncent.as<int>(),
+    cub::DeviceSelect::Flagged(nullptr, tmp, c.atom_idx.as<int>(), c.flags.as<int>(), c.cur_centres, c.ncent.as<int>(),
                                n, c.stream);
     if ((rc = c.cub_tmp.ensure(tmp))) return rc;
-    GG_CUDA(cub::DeviceSelect::Flagged(c.cub_tmp.p, tmp, c.atom_idx.as<int>(), c.flags.as<int>(), c.centres.as<int>(),
+    GG_CUDA(cub::DeviceSelect::Flagged(c.cub_tmp.p, tmp, c.atom_idx.as<int>(), c.flags.as<int>(), c.cur_centres,
                                        c.ncent.as<int>(), n, c.stream));
     int nc = 0;
     GG_CUDA(cudaMemcpyAsync(&nc, c.ncent.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));

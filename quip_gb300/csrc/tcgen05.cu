@@ -471,8 +471,7 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
         (rc = c.Wlo.ensure(es * nw)) || (rc = c.epart.ensure(sizeof(double) * (size_t)nc * ntiles_max)) ||
         (rc = c.Gbuf.ensure(sizeof(float) * nq)) || (rc = c.total.ensure(sizeof(int) * 4)))
         return rc;
-    int* err = c.total.as<int>() + 3;
-    GG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
+    int* err = c.total.as<int>() + 3;  // cleared at the start of the evaluation, read after it
     const int TB = 256;
     const unsigned nb = (unsigned)((nq + TB - 1) / TB);
     if (MODE == MODE_BF16X3)
@@ -490,7 +489,7 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
     else
         rc = gemm<MODE, EPI_KERNEL>(c, c.qlo.p, c.qlo.p, co.dXf32, co.dXf32, nc, Mp, Dp, ep, err, &ntiles);
     if (rc) return rc;
-    k_rowsum_scatter32<<<(nc + 127) / 128, 128, 0, c.stream>>>(nc, ntiles, c.epart.as<double>(), c.centres.as<int>(),
+    k_rowsum_scatter32<<<(nc + 127) / 128, 128, 0, c.stream>>>(nc, ntiles, c.epart.as<double>(), c.cur_centres,
                                                               c.eatom.as<double>());
     c.launches++;
     // GEMM2: G = W X, B operand = X^T rows (k = sparse index contiguous)
@@ -499,12 +498,7 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
         rc = gemm<MODE, EPI_STORE>(c, c.Wbuf.p, c.Wlo.p, co.dXThi, co.dXTlo, nc, Dp, Mp, ep2, err, nullptr);
     else
         rc = gemm<MODE, EPI_STORE>(c, c.Wbuf.p, c.Wbuf.p, co.dXTf32, co.dXTf32, nc, Dp, Mp, ep2, err, nullptr);
-    if (rc) return rc;
-    int herr = 0;
-    GG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    GG_CUDA(cudaStreamSynchronize(c.stream));
-    if (herr) GG_FAIL(GAPGPU_ERR_TIMEOUT, "tensor-core GEMM: a bounded mbarrier wait expired (code " + std::to_string(herr) + ")");
-    return GAPGPU_OK;
+    return rc;
 }
 
 }  // namespace

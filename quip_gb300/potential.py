@@ -133,6 +133,40 @@ class Potential:
         self.results = out
         return out
 
+    def calc_batch(self, structures, args_str=""):
+        """Energies, forces and virials of many independent structures in one GPU pass
+        (gapgpu_calc_batch).  Returns a list of dicts energy / force (N,3) / virial (3,3),
+        one per structure, each bit-identical to ``calc`` of that structure alone."""
+        ns = np.array([len(a) for a in structures], dtype=np.int32)
+        if len(ns) == 0:
+            return []
+        pos = np.ascontiguousarray(np.concatenate([a.positions for a in structures]), dtype=np.float64)
+        Z = np.ascontiguousarray(np.concatenate([a.numbers for a in structures]), dtype=np.int32)
+        lat = np.ascontiguousarray(np.concatenate([np.asfortranarray(a.lattice, dtype=np.float64).ravel(order="F")
+                                                   for a in structures]))
+        pbc = np.ascontiguousarray(np.concatenate([np.asarray(a.pbc, dtype=np.int32).reshape(3) for a in structures]))
+        E = np.zeros(len(ns))
+        F = np.zeros((len(pos), 3))
+        V = np.zeros((len(ns), 9))
+        _lib.check(self._L.gapgpu_calc_batch(self._ctx, len(ns), _lib.ptr(ns), _lib.ptr(pos), _lib.ptr(Z), _lib.ptr(lat),
+                                             _lib.ptr(pbc), _lib.ptr(E), _lib.ptr(F), _lib.ptr(V), args_str.encode()))
+        out, a0 = [], 0
+        for s, n in enumerate(ns):
+            out.append({"energy": float(E[s]), "force": F[a0:a0 + n], "virial": V[s].reshape(3, 3, order="F")})
+            a0 += n
+        return out
+
+    def set_option(self, key, value):
+        """Context options: graphs (CUDA-graph replay of repeated shapes), timing."""
+        _lib.check(self._L.gapgpu_context_set_option(self._ctx, key.encode(), int(value)))
+
+    def footprint(self, n_atoms, mean_neighbours=60.0):
+        """Estimated device bytes of one evaluation of n_atoms atoms."""
+        b = _lib.ctypes.c_int64()
+        _lib.check(self._L.gapgpu_model_footprint(self._model, _lib.PRECISIONS[self.precision], int(n_atoms),
+                                                  float(mean_neighbours), _lib.ctypes.byref(b)))
+        return b.value
+
     def calculate(self, atoms, properties=("energy", "forces", "stress")):
         """ASE-calculator view (quippy/quippy/potential.py:177-325): forces (N,3),
         stress = -virial / volume (potential.py:281-284), energies (local)."""
