@@ -8,6 +8,15 @@ kernel GEMMs, forces, virial) of one structure of the chosen workload:
            SOAP n_max=10 l_max=8 rc=5 A with 2 species channels (D=1891), 8000 sparse
            points, zeta=4, + distance_2b per species pair.
   sic8192  the same model on an 8192-atom cell (the size used for ncu captures).
+Besides the headline line's single-structure workload, the same line carries
+  batch    1024 independent triclinic Si/C structures (atom counts log-uniform in
+           [8, 2048], lengths 4-30 A, angles 70-110 deg, 1.8 A minimum separation) in one
+           batched evaluation, first call and CUDA-graph replay, against the plain FP64
+           per-structure loop on a sample;
+  serving  Poisson streams of E+F requests (sizes log-uniform 16-2048, drawn as for
+           batch) at several offered loads, served by the continuous-batching server
+           while 64 resident 512-atom Si MD replicas (1000 K, dt = 1 fs, 0.5 A skin)
+           step on their own stream; p50/p99 latency and throughput per load.
 Inputs are seeded synthetic structures and random GAP models (no dataset is published
 for this path).  `value` is timed with CUDA events on the launching stream with the
 inputs resident in HBM; `e2e` goes through the public C ABI (gapgpu_calc) with pinned
@@ -142,6 +151,66 @@ def cpu_reference(w, at, model_path, steps, warmup, sample_atoms=None):
             "seconds_per_sample": t}
 
 
+def measure_batch(path, precision, structs, fp64_sample=48):
+    """One batched evaluation of all structures (host arrays in and out, wall clock):
+    first call, then repeated calls with CUDA-graph replay; the per-structure FP64 loop
+    on a sample for comparison; the mixed result's error against it on that sample."""
+    from quip_gb300.potential import Potential
+    natoms = sum(len(a) for a in structs)
+    pot = Potential(param_filename=path, precision=precision)
+    t0 = time.perf_counter()
+    res = pot.calc_batch(structs)
+    first = time.perf_counter() - t0
+    pot.set_option("graphs", 1)
+    pot.set_option("timing", 0)
+    reps = []
+    for _ in range(4):   # direct, capture, replay, replay
+        t0 = time.perf_counter()
+        pot.calc_batch(structs)
+        reps.append(time.perf_counter() - t0)
+    p64 = Potential(param_filename=path, precision="fp64")
+    sample = structs[:fp64_sample]
+    t0 = time.perf_counter()
+    r64 = [p64.calc(a) for a in sample]
+    t64 = time.perf_counter() - t0
+    n64 = sum(len(a) for a in sample)
+    fmax = max(float(np.abs(r["force"] - b["force"]).max()) for r, b in zip(r64, res[:fp64_sample]) if len(r["force"]))
+    emax = max(abs(r["energy"] - b["energy"]) / max(1, len(a)) for r, b, a in zip(r64, res[:fp64_sample], sample))
+    return {"structures": len(structs), "atoms": natoms, "precision": precision,
+            "first_call_s": first, "atom_evals_per_s_first": natoms / first,
+            "graph_replay_s": min(reps[2:]), "atom_evals_per_s": natoms / min(reps[2:]),
+            "fp64_loop": {"structures": len(sample), "atoms": n64, "seconds": t64, "atom_evals_per_s": n64 / t64},
+            "speedup_vs_fp64_loop": (natoms / min(reps[2:])) / (n64 / t64),
+            "error_vs_fp64_sample": {"force_max_eV_per_A": fmax, "energy_per_atom_eV": emax},
+            "timing": "wall clock around gapgpu_calc_batch with host arrays (copies included)"}
+
+
+def measure_serving(path, precision, pool, loads, seconds, replicas=64, seed=11):
+    """Continuous-batching serving of Poisson request streams (sizes log-uniform 16-2048,
+    drawn from `pool`) next to resident MD replicas of 512-atom Si at 1000 K."""
+    from quip_gb300 import models as mdl
+    from quip_gb300.md import MDReplicas
+    from quip_gb300.potential import Potential
+    from quip_gb300.serving import Server, poisson_arrivals
+    reqpool = [a for a in pool if 16 <= len(a) <= 2048]
+    md = MDReplicas(Potential(param_filename=path, precision=precision),
+                    [mdl.si_diamond(4, rattle=0.05, seed=500 + k) for k in range(replicas)], dt=1.0, skin=0.5,
+                    temperature=1000.0, seed=seed)
+    srv = Server(path, precision=precision, workers=2, budget_bytes=24 << 30, md=md)
+    rng = np.random.default_rng(seed)
+    out = []
+    for rate in loads:
+        count = max(20, int(rate * seconds))
+        arrivals = poisson_arrivals(rate, count, seed=int(rate))
+        structs = [reqpool[i] for i in rng.integers(0, len(reqpool), count)]
+        _, st = srv.run(structs, arrivals, timeout=max(60.0, 10 * seconds))
+        st["offered_rps"] = rate
+        out.append(st)
+    c = md.counters()
+    return {"precision": precision, "md_replicas": replicas, "md_atoms": int(md.n_atoms.sum()), "workers": 2,
+            "loads": out, "md_counters": c}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -149,9 +218,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="sic32768", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x3", "tf32"])
+    ap.add_argument("--precision", default="tf32", choices=["fp64", "bf16x3", "tf32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip the FP64 comparison run (profiling)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 1024-structure batched measurement")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serving-loads", default="500,1500,4000", help="offered loads (requests/s)")
+    ap.add_argument("--serving-seconds", type=float, default=3.0)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -342,6 +415,16 @@ def main():
         except Exception as e:
             cpu = {"value": None, "error": str(e)[:160]}
 
+    batch = serving = None
+    if rank == 0 and w["kind"] == "sic" and not (args.no_batch and args.no_serving):
+        from quip_gb300 import models as mdl
+        pool = mdl.triclinic_batch(1024, n_min=8, n_max=2048, seed=7, workers=min(16, os.cpu_count() or 1))
+        if not args.no_batch:
+            batch = measure_batch(path, args.precision, pool)
+        if not args.no_serving:
+            serving = measure_serving(path, args.precision, pool, [float(x) for x in args.serving_loads.split(",")],
+                                      args.serving_seconds)
+
     if rank == 0:
         h2d = n * 3 * 8 + n * 4
         d2h = 8 + n * 3 * 8 + 9 * 8
@@ -359,7 +442,7 @@ def main():
                 "fp64": fp64, "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": "atom-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
-                "gpu_launches": int(run["launches"]), "clocks": clk.summary(),
+                "gpu_launches": int(run["launches"]), "clocks": clk.summary(), "batch": batch, "serving": serving,
                 "algorithmic_flops_per_atom": flops_atom, "wall_s": t_wall}
         print(json.dumps(line))
     if world > 1:

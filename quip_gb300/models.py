@@ -44,44 +44,71 @@ def si_primitive(a=5.43, rattle=0.0, seed=0):
     return Atoms([14, 14], pos, lattice=lat, pbc=True)
 
 
-def _place_uniform(n, lat, min_sep, rng, max_tries=200):
-    """Random sequential addition with a minimum separation (periodic, any lattice)."""
+def _place_uniform(n, lat, min_sep, rng, batch=256, max_stall=200):
+    """Random sequential addition with a minimum separation (periodic, any lattice),
+    in batches: a batch of uniform candidates is tested against every accepted atom in
+    the 27 neighbouring cells of a grid at least min_sep wide, then accepted in order
+    unless it clashes with an earlier candidate of the same batch.  Distances use the
+    nearest image in fractional coordinates, and all 27 images when the cell is less
+    than three grid cells wide."""
     g = np.linalg.inv(lat)
     widths = 1.0 / np.linalg.norm(g, axis=1)  # perpendicular widths
     nb = np.maximum(1, (widths / min_sep).astype(int))
-    grid = {}
-    frac_pos = np.zeros((n, 3))
+    small = nb.min() < 3
     shifts = np.array([[i, j, k] for i in (-1, 0, 1) for j in (-1, 0, 1) for k in (-1, 0, 1)])
+    ncell = int(np.prod(nb))
+    cap = 8
+    cell_atoms = np.full((ncell, cap), -1, dtype=np.int64)
+    cell_cnt = np.zeros(ncell, dtype=np.int64)
+    frac = np.zeros((n, 3))
     ms2 = min_sep * min_sep
-    for a in range(n):
-        for _ in range(max_tries):
-            f = rng.random(3)
-            c = tuple((f * nb).astype(int) % nb)
-            ok = True
-            cands = []
-            for s in shifts:
-                key = tuple((np.array(c) + s) % nb)
-                cands.extend(grid.get(key, ()))
-            if cands:
-                d = frac_pos[cands] - f
-                d -= np.round(d)
-                # check all images within one cell for small boxes
-                if min(nb) < 3:
-                    best = np.inf
-                    for s in shifts:
-                        dd = (d + s) @ lat.T
-                        best = min(best, np.min(np.einsum("ij,ij->i", dd, dd)))
-                    ok = best >= ms2
-                else:
-                    dd = d @ lat.T
-                    ok = np.min(np.einsum("ij,ij->i", dd, dd)) >= ms2
-            if ok:
-                frac_pos[a] = f
-                grid.setdefault(c, []).append(a)
-                break
-        else:
-            raise RuntimeError("could not place atom %d with min separation %.2f" % (a, min_sep))
-    return frac_pos @ lat.T
+    m, stall = 0, 0
+
+    def r2_of(d):  # squared Cartesian length of fractional differences (..., 3), nearest image
+        d = d - np.round(d)
+        if not small:
+            c = d @ lat.T
+            return np.einsum("...i,...i->...", c, c)
+        c = (d[..., None, :] + shifts) @ lat.T
+        return np.einsum("...i,...i->...", c, c).min(axis=-1)
+
+    while m < n:
+        k = min(batch, 2 * (n - m) + 8)
+        cand = rng.random((k, 3))
+        ci = (cand * nb).astype(np.int64) % nb
+        nc = (ci[:, None, :] + shifts[None]) % nb
+        lin = nc[..., 0] + nb[0] * (nc[..., 1] + nb[1] * nc[..., 2])
+        idx = cell_atoms[lin].reshape(k, -1)
+        valid = idx >= 0
+        r2 = np.where(valid, r2_of(frac[np.where(valid, idx, 0)] - cand[:, None, :]), np.inf)
+        sel = np.nonzero(r2.min(axis=1) >= ms2)[0]
+        took = 0
+        if len(sel):
+            C = cand[sel]
+            clash = r2_of(C[:, None, :] - C[None, :, :]) < ms2
+            np.fill_diagonal(clash, False)
+            taken = np.zeros(len(sel), dtype=bool)
+            for i in range(len(sel)):
+                if m + took >= n:
+                    break
+                if not (clash[i] & taken).any():
+                    taken[i] = True
+                    took += 1
+            for i in np.nonzero(taken)[0]:
+                c = int(lin[sel[i], 13])  # the candidate's own cell (zero shift)
+                if cell_cnt[c] == cap:
+                    cap *= 2
+                    grown = np.full((ncell, cap), -1, dtype=np.int64)
+                    grown[:, :cap // 2] = cell_atoms
+                    cell_atoms = grown
+                cell_atoms[c, cell_cnt[c]] = m
+                cell_cnt[c] += 1
+                frac[m] = C[i]
+                m += 1
+        stall = 0 if took else stall + 1
+        if stall > max_stall:
+            raise RuntimeError("could not place atom %d with min separation %.2f" % (m, min_sep))
+    return frac @ lat.T
 
 
 def random_binary(n=32768, density_gcc=3.2, min_sep=1.6, species=(14, 6), seed=0):
@@ -121,14 +148,35 @@ def random_triclinic(n, species=(14, 6), min_sep=1.8, max_density=0.08, rng=None
         if np.all(np.linalg.norm(lat, axis=0) <= 30.0 * 2.5):
             break
     Z = rng.choice(np.array(species), n)
-    pos = _place_uniform(n, lat, min_sep, rng)
+    for _ in range(20):  # random sequential addition can jam: retry in a 5% larger cell
+        try:
+            pos = _place_uniform(n, lat, min_sep, rng)
+            break
+        except RuntimeError:
+            lat = lat * 1.05
+    else:
+        raise RuntimeError("could not place %d atoms with minimum separation %.2f" % (n, min_sep))
     return Atoms(Z, pos, lattice=lat, pbc=True)
 
 
-def triclinic_batch(count=1024, n_min=8, n_max=2048, seed=0, **kw):
+def _triclinic_item(args):
+    k, n, seed, kw = args
+    return random_triclinic(int(n), rng=np.random.default_rng([seed, k]), **kw)
+
+
+def triclinic_batch(count=1024, n_min=8, n_max=2048, seed=0, workers=1, **kw):
+    """`count` random triclinic Si/C cells with atom counts log-uniform in [n_min, n_max].
+    Structure k is drawn from its own seed (seed, k), so the batch is the same whatever
+    the number of worker processes (spawned, so that no GPU context is forked)."""
     rng = np.random.default_rng(seed)
     ns = np.exp(rng.uniform(np.log(n_min), np.log(n_max), count)).astype(int)
-    return [random_triclinic(int(k), rng=rng, **kw) for k in ns]
+    items = [(k, int(n), seed, kw) for k, n in enumerate(ns)]
+    if workers <= 1:
+        return [_triclinic_item(it) for it in items]
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_triclinic_item, items, chunksize=8))
 
 
 # ------------------------------------------------------------------ GAP XML
