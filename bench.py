@@ -197,6 +197,9 @@ def measure_serving(path, precision, pool, loads, seconds, replicas=64, seed=11)
                     [mdl.si_diamond(4, rattle=0.05, seed=500 + k) for k in range(replicas)], dt=1.0, skin=0.5,
                     temperature=1000.0, seed=seed)
     srv = Server(path, precision=precision, workers=2, budget_bytes=24 << 30, md=md)
+    t0 = time.perf_counter()
+    srv.warmup(reqpool)
+    warm = time.perf_counter() - t0
     rng = np.random.default_rng(seed)
     out = []
     for rate in loads:
@@ -208,7 +211,7 @@ def measure_serving(path, precision, pool, loads, seconds, replicas=64, seed=11)
         out.append(st)
     c = md.counters()
     return {"precision": precision, "md_replicas": replicas, "md_atoms": int(md.n_atoms.sum()), "workers": 2,
-            "loads": out, "md_counters": c}
+            "warmup_s": warm, "loads": out, "md_counters": c}
 
 
 def main():
@@ -443,6 +446,7 @@ def main():
                 "e2e": {"value": e2e_value, "unit": "atom-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99))},
                 "gpu_launches": int(run["launches"]), "clocks": clk.summary(), "batch": batch, "serving": serving,
+                "autotune": _lib.tuning_report().strip().splitlines(),
                 "algorithmic_flops_per_atom": flops_atom, "wall_s": t_wall}
         print(json.dumps(line))
     if world > 1:

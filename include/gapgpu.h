@@ -115,8 +115,16 @@ int gapgpu_calc_batch(gapgpu_context* ctx, int nstruct, const int32_t* n_atoms, 
 
 /* Context options: "graphs" (0/1): replay the evaluation phase from a CUDA graph when a
  * call has the same shapes and buffers as the previous one (captured on the second such
- * call); "timing" (0/1): per-stage CUDA events (gapgpu_context_timings). */
+ * call); "timing" (0/1): per-stage CUDA events (gapgpu_context_timings); "priority"
+ * (0/1): run on a stream of default or highest scheduling priority (latency-critical
+ * requests next to background MD); "autotune" (0/1, default 1): time the tensor-core
+ * GEMM's tile candidates on the first GEMM of each new shape and keep the fastest. */
 int gapgpu_context_set_option(gapgpu_context* ctx, const char* key, int value);
+
+/* Text report of the autotuner's choices so far (one line per GEMM shape: chosen N tile
+ * and the time of every candidate).  Returns the report length; writes at most
+ * capacity-1 characters and a terminating NUL. */
+int gapgpu_tuning_report(char* buf, int capacity);
 
 /* Device memory one evaluation of n_atoms atoms with about mean_neighbours neighbours
  * each needs in a context of this precision (bytes, an estimate used for admission). */

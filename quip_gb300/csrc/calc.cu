@@ -459,6 +459,19 @@ int gapgpu_context_set_option(gapgpu_context* c, const char* key, int value) {
     const std::string k(key);
     if (k == "graphs") c->graph_mode = value ? 1 : 0;
     else if (k == "timing") c->timed = value != 0;
+    else if (k == "autotune") c->autotune = value != 0;
+    else if (k == "priority") {
+        // the context's own stream, recreated at the device's highest (value != 0) or
+        // default scheduling priority: kernels of higher-priority streams get free SMs first
+        if (!c->own_stream) GG_FAIL(GAPGPU_ERR_ARG, "priority applies to the context's own stream only");
+        int lo = 0, hi = 0;
+        GG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        GG_CUDA(cudaStreamSynchronize(c->stream));
+        cudaStream_t s = nullptr;
+        GG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, value ? hi : lo));
+        cudaStreamDestroy(c->stream);
+        c->stream = s;
+    }
     else GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_set_option: unknown option " + k);
     return GAPGPU_OK;
 }

@@ -65,6 +65,7 @@ struct gapgpu_context {
     cudaGraphExec_t graph = nullptr;
     std::vector<uintptr_t> graph_key, last_key;
     int graph_mode = 0;                       // 0: never, 1: capture on the second identical call
+    bool autotune = true;                     // time the GEMM tile candidates of a new shape once
     long long graph_hits = 0, graph_launches = 0;
     // stage timing (CUDA events): neighbour build, then the evaluation's stage boundaries
     bool timed = true, stage_valid = false, nbr_timed = false;

@@ -26,6 +26,9 @@
 #include <cmath>
 #include <vector>
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "context.h"
 
@@ -420,6 +423,40 @@ int pick_bn(int MODE, int N) {
     return 128;
 }
 
+// ---------------------------------------------------------------- autotuner
+// The first GEMM of a shape (mode, epilogue, N, K, log2 of the row count) times every
+// N tile that divides N and leaves at least two pipeline stages, on the real operands
+// (each candidate rewrites the same outputs), and keeps the fastest for the process --
+// the timing loop of IP_setup_parallel (src/Potentials/IP.f95:1092-1134) applied to
+// tile shapes.  Inside a stream capture no timing is possible: the heuristic decides.
+struct TuneKey {
+    int mode, epi, N, K, rb;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(mode, epi, N, K, rb) < std::tie(o.mode, o.epi, o.N, o.K, o.rb);
+    }
+};
+struct TuneEntry {
+    int bn;
+    std::vector<std::pair<int, float>> timings;  // (BN, ms)
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneEntry> g_tune;
+
+int rows_bucket(int rows) {
+    int b = 0;
+    while ((1 << b) < rows && b < 30) ++b;
+    return b;
+}
+
+template <int MODE>
+std::vector<int> bn_candidates(int N) {
+    std::vector<int> c;
+    if (N % 256 == 0 && Cfg<MODE, 256>::STAGES >= 2) c.push_back(256);
+    if (N % 192 == 0 && Cfg<MODE, 192>::STAGES >= 2) c.push_back(192);
+    c.push_back(128);
+    return c;
+}
+
 template <int MODE, int EPI, int BN>
 int launch_bn(gapgpu_context& c, const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
               const CUtensorMap& b1, int rows, int N, int kchunks, EpiParams ep, int* err) {
@@ -439,25 +476,72 @@ int launch_bn(gapgpu_context& c, const CUtensorMap& a0, const CUtensorMap& a1, c
 // One GEMM C = A B^T with the operand maps built here: A [rows x K] (planes a0, a1),
 // B [N x K] (planes b0, b1), both K-contiguous.
 template <int MODE, int EPI>
+int launch_any(gapgpu_context& c, int BN, const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
+               const CUtensorMap& b1, int rows, int N, int kchunks, const EpiParams& ep, int* err) {
+    if (BN == 256) return launch_bn<MODE, EPI, 256>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+    if (BN == 192) return launch_bn<MODE, EPI, 192>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+    return launch_bn<MODE, EPI, 128>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+}
+
+// One GEMM C = A B^T with the operand maps built here: A [rows x K] (planes a0, a1),
+// B [N x K] (planes b0, b1), both K-contiguous.
+template <int MODE, int EPI>
 int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows, int N, int K, EpiParams ep, int* err,
          int* ntiles_out) {
     const CUtensorMapDataType dt = MODE == MODE_BF16X3 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     const int es = MODE == MODE_BF16X3 ? 2 : 4, KB = 128 / es;
-    const int BN = pick_bn(MODE, N);
-    CUtensorMap a0, a1, b0, b1;
-    int rc;
-    if ((rc = make_map(&a0, a0p, dt, es, K, rows, KB)) || (rc = make_map(&b0, b0p, dt, es, K, N, KB, BN))) return rc;
-    if (MODE == MODE_BF16X3) {
-        if ((rc = make_map(&a1, a1p, dt, es, K, rows, KB)) || (rc = make_map(&b1, b1p, dt, es, K, N, KB, BN))) return rc;
-    } else {
-        a1 = a0;
-        b1 = b0;
-    }
-    if (ntiles_out) *ntiles_out = N / BN;
     const int kchunks = K / KB;
-    if (BN == 256) return launch_bn<MODE, EPI, 256>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
-    if (BN == 192) return launch_bn<MODE, EPI, 192>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
-    return launch_bn<MODE, EPI, 128>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+    int rc;
+    auto maps = [&](int BN, CUtensorMap& a0, CUtensorMap& a1, CUtensorMap& b0, CUtensorMap& b1) {
+        int r;
+        if ((r = make_map(&a0, a0p, dt, es, K, rows, KB)) || (r = make_map(&b0, b0p, dt, es, K, N, KB, BN))) return r;
+        if (MODE == MODE_BF16X3) {
+            if ((r = make_map(&a1, a1p, dt, es, K, rows, KB)) || (r = make_map(&b1, b1p, dt, es, K, N, KB, BN))) return r;
+        } else {
+            a1 = a0;
+            b1 = b0;
+        }
+        return (int)GAPGPU_OK;
+    };
+    const TuneKey key{MODE, EPI, N, K, rows_bucket(rows)};
+    int BN = 0;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) BN = it->second.bn;
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    GG_CUDA(cudaStreamIsCapturing(c.stream, &cap));
+    if (!BN && c.autotune && cap == cudaStreamCaptureStatusNone) {
+        TuneEntry te{0, {}};
+        cudaEvent_t e0, e1;
+        GG_CUDA(cudaEventCreate(&e0));
+        GG_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        for (int bn : bn_candidates<MODE>(N)) {
+            CUtensorMap a0, a1, b0, b1;
+            if ((rc = maps(bn, a0, a1, b0, b1))) return rc;
+            if ((rc = launch_any<MODE, EPI>(c, bn, a0, a1, b0, b1, rows, N, kchunks, ep, err))) return rc;  // warm
+            GG_CUDA(cudaEventRecord(e0, c.stream));
+            if ((rc = launch_any<MODE, EPI>(c, bn, a0, a1, b0, b1, rows, N, kchunks, ep, err))) return rc;
+            GG_CUDA(cudaEventRecord(e1, c.stream));
+            GG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            te.timings.push_back({bn, ms});
+            if (ms < best) { best = ms; te.bn = bn; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        BN = te.bn;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[key] = te;
+    }
+    if (!BN) BN = pick_bn(MODE, N);
+    CUtensorMap a0, a1, b0, b1;
+    if ((rc = maps(BN, a0, a1, b0, b1))) return rc;
+    if (ntiles_out) *ntiles_out = N / BN;
+    return launch_any<MODE, EPI>(c, BN, a0, a1, b0, b1, rows, N, kchunks, ep, err);
 }
 
 template <int MODE>
@@ -563,3 +647,26 @@ int gp_mixed(gapgpu_context& c, const Coordinate& co, int nc, int precision) {
 }
 
 }  // namespace gapgpu
+
+extern "C" int gapgpu_tuning_report(char* buf, int capacity) {
+    using namespace gapgpu;
+    std::string out;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const auto& kv : g_tune) {
+        const TuneKey& k = kv.first;
+        out += std::string(k.mode == MODE_BF16X3 ? "bf16x3" : "tf32") + (k.epi == EPI_KERNEL ? " kernel" : " store") +
+               " N=" + std::to_string(k.N) + " K=" + std::to_string(k.K) + " rows<=2^" + std::to_string(k.rb) +
+               " BN=" + std::to_string(kv.second.bn) + " [";
+        for (size_t i = 0; i < kv.second.timings.size(); ++i) {
+            char t[48];
+            std::snprintf(t, sizeof t, "%s%d:%.3fms", i ? " " : "", kv.second.timings[i].first, kv.second.timings[i].second);
+            out += t;
+        }
+        out += "]\n";
+    }
+    if (buf && capacity > 0) {
+        std::strncpy(buf, out.c_str(), (size_t)capacity - 1);
+        buf[capacity - 1] = 0;
+    }
+    return (int)out.size();
+}

@@ -64,6 +64,7 @@ class Server:
         self.pots = [Potential(param_filename=param_filename, precision=precision) for _ in range(max(1, workers))]
         for p in self.pots:
             p.set_option("timing", 0)
+            p.set_option("priority", 1)   # requests ahead of the background MD stream
         self.md = md
         self.mean_neighbours = mean_neighbours
         if budget_bytes is None:
@@ -78,6 +79,33 @@ class Server:
 
     def admit(self, queue):
         return admit_prefix(queue, lambda r: self.footprint(r.atoms), self.share)
+
+    def warmup(self, structures, max_atoms=None):
+        """Run batches of doubling size (up to one worker's memory share) through every
+        worker before serving: device buffers reach their final size and the GEMM
+        autotuner has seen every row count, so no request later waits on an allocation
+        (cudaMalloc/cudaFree synchronise the whole device) or a tuning run."""
+        if not structures:
+            return
+        per_atom = max(1, self.pots[0].footprint(1 << 16, self.mean_neighbours) >> 16)
+        cap = self.share // per_atom if max_atoms is None else max_atoms
+        order = sorted(structures, key=len)
+        target = 8
+        while True:
+            batch, n = [], 0
+            for a in order:
+                if n + len(a) > target:
+                    break
+                batch.append(a)
+                n += len(a)
+            if not batch:
+                batch = order[:1]
+            for p in self.pots:
+                p.calc_batch(batch)
+            if target >= cap or n >= sum(len(a) for a in order):
+                break
+            target = min(2 * target, cap)
+            order = order[len(batch):] + order[:len(batch)]
 
     def run(self, structures, arrivals, md_steps_per_tick=1, timeout=600.0):
         """Serve requests for `structures` arriving at times `arrivals` (s, from start).
