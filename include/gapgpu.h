@@ -150,6 +150,12 @@ int gapgpu_md_counters(const gapgpu_md* md, int64_t* steps, int64_t* rebuilds, i
 gapgpu_context* gapgpu_md_context(gapgpu_md* md);
 void gapgpu_md_destroy(gapgpu_md* md);
 
+/* Failure-detection self-test: a kernel waits on a device barrier that is never
+ * signalled, with the bounded wait the tensor-core GEMMs use, `limit` polls long
+ * (1..2^24).  Returns GAPGPU_ERR_TIMEOUT with a message once the wait has given up; the
+ * context stays usable.  Used by the tests; no counterpart in the reference. */
+int gapgpu_selftest_bounded_wait(gapgpu_context* ctx, int64_t limit);
+
 /* Wait for the context's stream. */
 int gapgpu_context_sync(gapgpu_context* ctx);
 

@@ -296,7 +296,7 @@ int check_device_flags(gapgpu_context& c) {
     int f[4] = {0, 0, 0, 0};
     GG_CUDA(cudaMemcpy(f, c.total.p, sizeof f, cudaMemcpyDeviceToHost));
     if (f[2] & 2) GG_FAIL(GAPGPU_ERR_ATOMS, "connection_calc_dists: atoms overlap exactly (distance below 1e-10)");
-    if (f[3]) GG_FAIL(GAPGPU_ERR_TIMEOUT, "tensor-core GEMM: a bounded mbarrier wait expired (code " + std::to_string(f[3]) + ")");
+    if (f[3]) GG_FAIL(GAPGPU_ERR_TIMEOUT, "a bounded device-side mbarrier wait expired (code " + std::to_string(f[3]) + ")");
     return GAPGPU_OK;
 }
 

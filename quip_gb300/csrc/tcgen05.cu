@@ -89,6 +89,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile
     return false;
 }
 
+// Diagnostic: one warp waits on an mbarrier that nothing arrives on, with the bounded
+// wait of the GEMM kernels and a caller-chosen iteration limit; on expiry it records the
+// error code and returns.  No asynchronous copy or MMA is in flight.
+__global__ void k_wait_probe(long long limit, int* err) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ volatile int abort_flag;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    for (long long i = 0; i < limit; ++i) {
+        if (mbar_try(&bar, 0)) return;  // never completes: no thread arrives
+        if (abort_flag) return;
+    }
+    abort_flag = 1;
+    atomicOr(err, 8);
+}
+
 __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* tm, int c0, int c1, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
@@ -669,4 +689,17 @@ extern "C" int gapgpu_tuning_report(char* buf, int capacity) {
         buf[capacity - 1] = 0;
     }
     return (int)out.size();
+}
+
+extern "C" int gapgpu_selftest_bounded_wait(gapgpu_context* c, int64_t limit) {
+    using namespace gapgpu;
+    if (!c || limit < 1 || limit > (1LL << 24)) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_selftest_bounded_wait: bad argument");
+    int rc;
+    if ((rc = c->total.ensure(sizeof(int) * 4))) return rc;
+    int* err = c->total.as<int>() + 3;
+    GG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+    k_wait_probe<<<1, 32, 0, c->stream>>>(limit, err);
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaStreamSynchronize(c->stream));
+    return check_device_flags(*c);
 }

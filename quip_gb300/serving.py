@@ -23,6 +23,7 @@ import time
 
 import numpy as np
 
+from ._lib import GapGpuError
 from .potential import Potential
 
 
@@ -131,6 +132,21 @@ class Server:
                         queue.append(pending.popleft())
                     self._cv.notify_all()
 
+        def evaluate(pot, batch):
+            """The batch in one pass; if that fails (a structure the library rejects:
+            overlapping atoms, NaN positions, ...), each request alone, so that only
+            the bad ones fail -- their result is {"error": message}."""
+            try:
+                return pot.calc_batch([r.atoms for r in batch])
+            except GapGpuError:
+                out = []
+                for r in batch:
+                    try:
+                        out.append(pot.calc_batch([r.atoms])[0])
+                    except GapGpuError as e:
+                        out.append({"error": str(e)})
+                return out
+
         def worker(pot):
             try:
                 while not stop.is_set():
@@ -143,7 +159,7 @@ class Server:
                     if not batch:
                         continue
                     ta = clock()
-                    res = pot.calc_batch([r.atoms for r in batch])
+                    res = evaluate(pot, batch)
                     td = clock()
                     with self._cv:
                         for r, x in zip(batch, res):
@@ -182,10 +198,11 @@ class Server:
         wall = clock()
         if state["error"] is not None:
             raise state["error"]
-        done = [r for r in reqs if r.done is not None]
+        done = [r for r in reqs if r.done is not None and "error" not in r.result]
         lat = np.array([r.done - r.arrival for r in done]) if done else np.zeros(1)
         atoms = sum(len(r.atoms) for r in done)
-        stats = {"requests": len(done), "wall_s": wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+        stats = {"requests": len(done), "failed": sum(1 for r in reqs if r.result is not None and "error" in r.result),
+                 "wall_s": wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                  "p99_ms": 1e3 * float(np.percentile(lat, 99)), "mean_ms": 1e3 * float(lat.mean()),
                  "atom_evals_per_s": atoms / wall if wall > 0 else 0.0, "batches": state["batches"],
                  "mean_batch_atoms": float(np.mean(state["batch_atoms"])) if state["batch_atoms"] else 0.0,

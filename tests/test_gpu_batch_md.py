@@ -154,3 +154,36 @@ def test_serving_results_are_the_same_alone_and_in_the_mix(sic_gap):
         a = alone.calc(r.atoms)
         assert abs(a["energy"] - r.result["energy"]) <= 1e-12 * max(1.0, abs(a["energy"]))
         assert np.abs(a["force"] - r.result["force"]).max() <= 1e-12
+
+
+def test_serving_isolates_a_bad_request(sic_gap):
+    """A request the library rejects (two atoms on top of each other) fails alone with
+    its error; every other request of the same batch is served."""
+    from quip_gb300.serving import Server
+    rng = np.random.default_rng(12)
+    structs = [models.random_triclinic(int(k), rng=rng) for k in (30, 50, 40)]
+    bad = structs[1].copy()
+    bad.positions[3] = bad.positions[0]
+    structs[1] = bad
+    srv = Server(sic_gap, precision="fp64", workers=1, budget_bytes=1 << 30)
+    reqs, stats = srv.run(structs, np.zeros(len(structs)))
+    assert "overlap" in reqs[1].result["error"]
+    assert stats["failed"] == 1 and stats["requests"] == 2
+    alone = _pot(sic_gap)
+    for k in (0, 2):
+        assert reqs[k].result["energy"] == alone.calc(structs[k])["energy"]
+
+
+def test_bounded_device_wait_reports_timeout_and_context_survives(sic_gap):
+    """Failure detection without a fault: a kernel waits on a barrier nothing signals;
+    the wait gives up after its bound, the host reads GAPGPU_ERR_TIMEOUT, and the same
+    context then evaluates normally."""
+    from quip_gb300 import _lib
+    pot = _pot(sic_gap, "tf32")
+    at = models.random_triclinic(40, rng=np.random.default_rng(3))
+    ref = pot.calc(at)["energy"]
+    rc = pot._L.gapgpu_selftest_bounded_wait(pot._ctx, 20000)
+    assert rc == _lib.ERR_TIMEOUT
+    assert b"bounded device-side" in pot._L.gapgpu_last_error()
+    assert pot.calc(at)["energy"] == ref
+
