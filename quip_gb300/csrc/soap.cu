@@ -220,7 +220,7 @@ __device__ __forceinline__ int l_of_lm(int lm) {
     return l;
 }
 
-constexpr int FWD_THREADS = 128;
+constexpr int FWD_THREADS = 256;
 constexpr int TC = 32;   // neighbours staged per chunk in the forward kernel
 constexpr int TCB = 16;  // ... and in the backward kernel (dual Ylm staging is 4x larger)
 
@@ -289,12 +289,55 @@ __device__ __forceinline__ void load_tab(const R* __restrict__ tab, R* K, int n)
     for (int k = threadIdx.x; k < n; k += blockDim.x) K[k] = tab[k];
 }
 
+// A flattened loop index k = i * B + j walked with a fixed stride S: (i, j) advance
+// without an integer division per step (S / B and S % B are formed once).
+struct Walk2 {
+    int i, j, si, sj, B;
+    __device__ __forceinline__ Walk2(int k, int S, int B_) : B(B_) {
+        i = k / B;
+        j = k - i * B;
+        si = S / B;
+        sj = S - si * B;
+    }
+    __device__ __forceinline__ void next() {
+        i += si;
+        j += sj;
+        if (j >= B) {
+            j -= B;
+            ++i;
+        }
+    }
+};
+
+__device__ __forceinline__ void load4(const float* p, float& a, float& b, float& c, float& d) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    a = v.x; b = v.y; c = v.z; d = v.w;
+}
+__device__ __forceinline__ void load4(const double* p, double& a, double& b, double& c, double& d) {
+    const double2 u = reinterpret_cast<const double2*>(p)[0], v = reinterpret_cast<const double2*>(p)[1];
+    a = u.x; b = u.y; c = v.x; d = v.y;
+}
+
+// Accumulator items a forward thread keeps in registers: FQ_SMALL for bases of up to
+// FQ_SMALL * 256 items (s, lm, 4 radial functions), FQ_LARGE beyond.
+constexpr int FQ_SMALL = 2, FQ_LARGE = 8;
+
+// Size (elements) of the forward kernel's shared region: staging, ct or power spectrum.
+__host__ __device__ __forceinline__ int fwd_region(const SoapConst& sc) {
+    const int L = sc.l_max + 1, L2 = L * L, NMP = nmp_of(sc.n_max);
+    int r = TC * L2 + TC * L * NMP + TC + TC * DS;
+    r = r > sc.n_species * L2 * NMP ? r : sc.n_species * L2 * NMP;
+    r = r > sc.n_pairs * L ? r : sc.n_pairs * L;
+    return (r + 3) & ~3;
+}
+
 // Forward: one block per centre.  Densities are accumulated in the collocation basis
-// ct[s][lm][a] = sum_j fc rho_l(r_j, r_a) Y_lm(r^_j); the orthonormalising transform
-// c[s][n][lm] = sum_a T_an ct[s][lm][a] is applied once per centre.  In the mixed path
-// everything is FP32 except the norm reduction (per-thread FP32 partial sums combined
-// in FP64) and 1/|p|.
-template <class R>
+// ct[s][lm][a] = sum_j fc rho_l(r_j, r_a) Y_lm(r^_j): each thread owns up to FQ items
+// (s, lm, 4 consecutive a) in registers for the whole neighbour loop.  The
+// orthonormalising transform c[s][n][lm] = sum_a T_an ct[s][lm][a] is applied once per
+// centre by one thread per (s, lm).  In the mixed path everything is FP32 except the
+// norm reduction (per-thread FP32 partial sums combined in FP64) and 1/|p|.
+template <class R, int FQ>
 __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, const R* __restrict__ tab, int nc,
                                                                const int* __restrict__ centres, const int* __restrict__ Z,
                                                                const int* __restrict__ off, const int* __restrict__ nj,
@@ -306,20 +349,40 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     const int atom = centres[ci];
     const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, NMP = nmp_of(nm), NS = sc.n_species;
     const SoapTab tb = soap_tab(nm, L);
+    // [K][cs][region]: the region holds the neighbour staging during the loop, then the
+    // accumulators ct for the transform, then the power spectrum (ct is dead by then)
     R* K = reinterpret_cast<R*>(smem_raw);           // tb.size
-    R* ct = K + tb.size;                              // NS * L2 * NMP
-    R* cs = ct + NS * L2 * NMP;                       // NS * nm * L2
-    R* Ysm = cs + NS * nm * L2;                       // TC * L2          (power spectrum reuses this region)
+    R* cs = K + tb.size;                              // NS * nm * L2
+    R* Ysm = cs + ((NS * nm * L2 + 3) & ~3);          // TC * L2
     R* Ism = Ysm + TC * L2;                           // TC * L * NMP
     R* fcs = Ism + TC * L * NMP;                      // TC
     R* dsm = fcs + TC;                                // TC * DS
-    const int stage = TC * L2 + TC * L * NMP + TC + TC * DS, ps_len = sc.n_pairs * L;
-    int* spc = reinterpret_cast<int*>(Ysm + (stage > ps_len ? stage : ps_len));  // TC
+    R* ct = Ysm;                                      // NS * L2 * NMP, after the loop
+    const int region = fwd_region(sc);
+    int* spc = reinterpret_cast<int*>(Ysm + region);  // TC
     int* lst = spc + TC;                              // NS * TC
     int* lcnt = lst + NS * TC;                        // NS
-    const int tid = threadIdx.x;
+    unsigned char* lofm = reinterpret_cast<unsigned char*>(lcnt + NS);  // L2
+    const int tid = threadIdx.x, bd = blockDim.x;
     load_tab(tab, K, tb.size);
-    for (int k = tid; k < NS * L2 * NMP; k += blockDim.x) ct[k] = 0;
+    for (int k = tid; k < L2; k += bd) lofm[k] = (unsigned char)l_of_lm(k);
+    const int NA4 = NMP / 4, items = NS * L2 * NA4;
+
+    R acc[FQ][4];
+    int own_s[FQ], own_lm[FQ], own_a4[FQ];
+#pragma unroll
+    for (int q = 0; q < FQ; ++q) {
+        const int k = tid + q * bd;
+        own_s[q] = -1;
+        own_lm[q] = own_a4[q] = 0;
+        if (k < items) {
+            own_s[q] = k / (L2 * NA4);
+            const int rem = k - own_s[q] * L2 * NA4;
+            own_lm[q] = rem / NA4;
+            own_a4[q] = rem - own_lm[q] * NA4;
+        }
+        acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0;
+    }
     const R alpha = (R)sc.alpha;
     const int p0 = off[atom], p1 = off[atom + 1];
     for (int base = p0; base < p1; base += TC) {
@@ -331,59 +394,78 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
             stage_neighbour<R>(sc, nd[base + t], dsm + DS * t, fcs + t, (R*)nullptr);
         }
         __syncthreads();
-        for (int k = tid; k < cnt * L; k += blockDim.x) {
-            const int t = k / L, m = k % L;
-            if (spc[t] < 0) continue;
-            const R* u = dsm + DS * t;
-            ylm_column<R>(m, L, u[0], u[1], u[2], K, tb, Ysm + t * L2);
-        }
-        for (int k = tid; k < cnt * NMP; k += blockDim.x) {
-            const int t = k / NMP, a = k % NMP;
-            if (spc[t] < 0) continue;
-            R* out = Ism + t * L * NMP + a;
-            if (a >= nm) {
-                for (int l = 0; l < L; ++l) out[l * NMP] = 0;
-                continue;
+        if (tid < cnt * L) {
+            Walk2 w(tid, bd, L);
+            for (; w.i < cnt; w.next()) {
+                if (spc[w.i] < 0) continue;
+                const R* u = dsm + DS * w.i;
+                ylm_column<R>(w.j, L, u[0], u[1], u[2], K, tb, Ysm + w.i * L2);
             }
-            radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, fcs[t], out, (R*)nullptr, NMP);
+        }
+        if (tid < cnt * NMP) {
+            Walk2 w(tid, bd, NMP);
+            for (; w.i < cnt; w.next()) {
+                const int t = w.i, a = w.j;
+                if (spc[t] < 0) continue;
+                R* out = Ism + t * L * NMP + a;
+                if (a >= nm) {
+                    for (int l = 0; l < L; ++l) out[l * NMP] = 0;
+                    continue;
+                }
+                radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, fcs[t], out, (R*)nullptr, NMP);
+            }
         }
         __syncthreads();
-        // ct[s][lm][a..a+3] += sum_{t in species s} Y[t][lm] I[t][l][a..a+3]
-        const int NA4 = NMP / 4;
-        for (int k = tid; k < NS * L2 * NA4; k += blockDim.x) {
-            const int s = k / (L2 * NA4), rem = k % (L2 * NA4), lm = rem / NA4, a4 = rem % NA4;
-            const int l = l_of_lm(lm);
-            R a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        // acc[s][lm][a..a+3] += sum_{t in species s} Y[t][lm] I[t][l][a..a+3]
+#pragma unroll
+        for (int q = 0; q < FQ; ++q) {
+            const int s = own_s[q];
+            if (s < 0) continue;
+            const int lm = own_lm[q], l = lofm[lm], a4 = own_a4[q];
             const int nt = lcnt[s];
             const int* ls = lst + s * TC;
-            for (int q = 0; q < nt; ++q) {
-                const int t = ls[q];
+            for (int qq = 0; qq < nt; ++qq) {
+                const int t = ls[qq];
                 const R y = Ysm[t * L2 + lm];
-                const R* iv = Ism + (t * L + l) * NMP + 4 * a4;
-                a0 += y * iv[0]; a1 += y * iv[1]; a2 += y * iv[2]; a3 += y * iv[3];
+                R i0, i1, i2, i3;
+                load4(Ism + (t * L + l) * NMP + 4 * a4, i0, i1, i2, i3);
+                acc[q][0] += y * i0; acc[q][1] += y * i1; acc[q][2] += y * i2; acc[q][3] += y * i3;
             }
-            R* o = ct + (s * L2 + lm) * NMP + 4 * a4;
-            o[0] += a0; o[1] += a1; o[2] += a2; o[3] += a3;
         }
     }
+    __syncthreads();  // the staging area becomes ct
+#pragma unroll
+    for (int q = 0; q < FQ; ++q) {
+        if (own_s[q] < 0) continue;
+        R* o = ct + (own_s[q] * L2 + own_lm[q]) * NMP + 4 * own_a4[q];
+        o[0] = acc[q][0]; o[1] = acc[q][1]; o[2] = acc[q][2]; o[3] = acc[q][3];
+    }
     __syncthreads();
-    // c[s][n][lm] = sum_a T_an ct[s][lm][a]  (+ central atom at l = 0)
+    // c[s][n][lm] = sum_a T_an ct[s][lm][a]  (+ central atom at l = 0): one thread per (s, lm)
     const int zc = Z[atom];
-    for (int k = tid; k < NS * nm * L2; k += blockDim.x) {
-        const int s = k / (nm * L2), rem = k % (nm * L2), n = rem / L2, lm = rem % L2;
+    for (int k = tid; k < NS * L2; k += bd) {
+        const int s = k / L2, lm = k - s * L2;
         const R* v = ct + (s * L2 + lm) * NMP;
-        R acc = 0;
-        for (int a = 0; a < nm; ++a) acc += K[tb.T + a * nm + n] * v[a];
-        if (lm == 0 && (sc.centre_all || sc.species_Z[s] == zc || sc.species_Z[s] == 0)) acc += K[tb.cr + n];
-        cs[k] = acc;
+        R va[MAX_NMAX];
+#pragma unroll
+        for (int a = 0; a < MAX_NMAX; ++a) va[a] = a < nm ? v[a] : (R)0;
+        const bool centre = lm == 0 && (sc.centre_all || sc.species_Z[s] == zc || sc.species_Z[s] == 0);
+        for (int n = 0; n < nm; ++n) {
+            R x = 0;
+#pragma unroll
+            for (int a = 0; a < MAX_NMAX; ++a)
+                if (a < nm) x += K[tb.T + a * nm + n] * va[a];
+            if (centre) x += K[tb.cr + n];
+            cs[(s * nm + n) * L2 + lm] = x;
+        }
     }
     __syncthreads();
     R* cg = c_out + (size_t)ci * sc.ncomp;
-    for (int k = tid; k < sc.ncomp; k += blockDim.x) cg[k] = cs[k];
+    for (int k = tid; k < sc.ncomp; k += bd) cg[k] = cs[k];
     // power spectrum: one item per (ia, jb) pair, all l
     R* ps = Ysm;
     R ssr = 0;
-    for (int pr = tid; pr < sc.n_pairs; pr += blockDim.x) {
+    for (int pr = tid; pr < sc.n_pairs; pr += bd) {
         int ia, jb;
         decode_pair(pr, ia, jb);
         const R* ca = cs + ia * L2;
@@ -410,7 +492,7 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     const R inv = (R)s_inv;
     const int np = sc.n_pairs * L;
     R* qg = q_out + (size_t)ci * sc.dpad;
-    for (int k = tid; k < sc.dpad; k += blockDim.x) {
+    for (int k = tid; k < sc.dpad; k += bd) {
         R v;
         if (k < np) v = ps[k] * inv;
         else if (k == np) v = (R)sc.sigma0;
@@ -419,7 +501,7 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     }
 }
 
-constexpr int BWD_THREADS = 128;
+constexpr int BWD_THREADS = 256;
 constexpr int BWD_WARPS = BWD_THREADS / 32;
 
 // Shared-memory plan of the backward kernel (elements of R): constant block, h, then a
@@ -476,14 +558,16 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
     int* spc = reinterpret_cast<int*>(K + pl.ints_at);  // TCB
     int* lst = spc + TCB;                               // NS * TCB
     int* lcnt = lst + NS * TCB;                         // NS
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    unsigned char* lofm = reinterpret_cast<unsigned char*>(lcnt + NS);  // L2
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, bd = blockDim.x;
     load_tab(tab, K, tb.size);
+    for (int k = tid; k < L2; k += bd) lofm[k] = (unsigned char)l_of_lm(k);
     const R* cg = c_in + (size_t)ci * sc.ncomp;
-    for (int k = tid; k < sc.ncomp; k += blockDim.x) cs[k] = cg[k];
+    for (int k = tid; k < sc.ncomp; k += bd) cs[k] = cg[k];
     const R* qg = q_in + (size_t)ci * sc.dpad;
     const R* gg = G + (size_t)ci * sc.dpad;
     R part = 0;
-    for (int k = tid; k < np; k += blockDim.x) part += qg[k] * gg[k];
+    for (int k = tid; k < np; k += bd) part += qg[k] * gg[k];
     typedef cub::BlockReduce<double, BWD_THREADS> BR;
     __shared__ typename BR::TempStorage tmps;
     const double tot = BR(tmps).Sum((double)part);
@@ -494,7 +578,7 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
     }
     __syncthreads();
     const R sq = (R)s_qg, inv = (R)s_inv;
-    for (int pr = tid; pr < sc.n_pairs; pr += blockDim.x) {
+    for (int pr = tid; pr < sc.n_pairs; pr += bd) {
         int ia, jb;
         decode_pair(pr, ia, jb);
         const R f0 = ia != jb ? (R)1.41421356237309504880 : (R)2;
@@ -505,26 +589,39 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
         }
     }
     __syncthreads();
-    for (int k = tid; k < sc.ncomp; k += blockDim.x) {
-        const int a = k / L2, lm = k - a * L2;
-        const int l = l_of_lm(lm);
-        R acc = 0;
-        int idx = (a * (a + 1) / 2) * L + l;  // pair (a, b = 0)
-        for (int b = 0; b <= a; ++b, idx += L) acc += dp[idx] * cs[b * L2 + lm];
-        idx = ((a + 1) * (a + 2) / 2 + a) * L + l;  // pair (b = a + 1, a)
-        for (int b = a + 1; b < NN; ++b) {
-            acc += dp[idx] * cs[b * L2 + lm];
-            idx += (b + 1) * L;
+    if (tid < sc.ncomp) {
+        Walk2 w(tid, bd, L2);
+        for (; w.i < NN; w.next()) {
+            const int a = w.i, lm = w.j, l = lofm[lm];
+            R acc = 0;
+            int idx = (a * (a + 1) / 2) * L + l;  // pair (a, b = 0)
+            const R* cb = cs + lm;
+            for (int b = 0; b <= a; ++b, idx += L) acc += dp[idx] * cb[b * L2];
+            idx = ((a + 1) * (a + 2) / 2 + a) * L + l;  // pair (b = a + 1, a)
+            for (int b = a + 1; b < NN; ++b) {
+                acc += dp[idx] * cb[b * L2];
+                idx += (b + 1) * L;
+            }
+            dc[a * L2 + lm] = acc;
         }
-        dc[k] = acc;
     }
     __syncthreads();
-    for (int k = tid; k < NS * L2 * NMP; k += blockDim.x) {
-        const int s = k / (L2 * NMP), rem = k % (L2 * NMP), lm = rem / NMP, a = rem % NMP;
-        R acc = 0;
-        if (a < nm)
-            for (int n = 0; n < nm; ++n) acc += K[tb.T + a * nm + n] * dc[(s * nm + n) * L2 + lm];
-        hs[k] = acc;
+    // h[s][lm][a] = sum_n T_an dE/dc[s][n][lm]: one thread per (s, lm)
+    for (int k = tid; k < NS * L2; k += bd) {
+        const int s = k / L2, lm = k - s * L2;
+        R vn[MAX_NMAX];
+#pragma unroll
+        for (int n = 0; n < MAX_NMAX; ++n) vn[n] = n < nm ? dc[(s * nm + n) * L2 + lm] : (R)0;
+        R* o = hs + (s * L2 + lm) * NMP;
+        for (int a = 0; a < NMP; ++a) {
+            R x = 0;
+            if (a < nm) {
+#pragma unroll
+                for (int n = 0; n < MAX_NMAX; ++n)
+                    if (n < nm) x += K[tb.T + a * nm + n] * vn[n];
+            }
+            o[a] = x;
+        }
     }
     const R alpha = (R)sc.alpha;
     const int p0 = off[atom], p1 = off[atom + 1];
@@ -537,22 +634,27 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
             stage_neighbour<R>(sc, nd[base + t], dsm + DS * t, fcs + t, dfcs + t);
         }
         __syncthreads();
-        for (int k = tid; k < cnt * L; k += blockDim.x) {
-            const int t = k / L, m = k % L;
-            if (spc[t] < 0) continue;
-            const R* u = dsm + DS * t;
-            ylm_column_grad<R>(m, L, u[0], u[1], u[2], u[3], K, tb, Yd + t * L2);
-        }
-        for (int k = tid; k < cnt * NMP; k += blockDim.x) {
-            const int t = k / NMP, a = k % NMP;
-            if (spc[t] < 0) continue;
-            R* o = Ism + t * L * NMP + a;
-            R* od = dIsm + t * L * NMP + a;
-            if (a >= nm) {
-                for (int l = 0; l < L; ++l) { o[l * NMP] = 0; od[l * NMP] = 0; }
-                continue;
+        if (tid < cnt * L) {
+            Walk2 w(tid, bd, L);
+            for (; w.i < cnt; w.next()) {
+                if (spc[w.i] < 0) continue;
+                const R* u = dsm + DS * w.i;
+                ylm_column_grad<R>(w.j, L, u[0], u[1], u[2], u[3], K, tb, Yd + w.i * L2);
             }
-            radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, (R)1, o, od, NMP);
+        }
+        if (tid < cnt * NMP) {
+            Walk2 w(tid, bd, NMP);
+            for (; w.i < cnt; w.next()) {
+                const int t = w.i, a = w.j;
+                if (spc[t] < 0) continue;
+                R* o = Ism + t * L * NMP + a;
+                R* od = dIsm + t * L * NMP + a;
+                if (a >= nm) {
+                    for (int l = 0; l < L; ++l) { o[l * NMP] = 0; od[l * NMP] = 0; }
+                    continue;
+                }
+                radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, (R)1, o, od, NMP);
+            }
         }
         __syncthreads();
         for (int t = wid; t < cnt; t += BWD_WARPS) {
@@ -563,7 +665,7 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
             const R f = fcs[t], df = dfcs[t];
             R fx = 0, fy = 0, fz = 0;
             for (int lm = lane; lm < L2; lm += 32) {
-                const int l = l_of_lm(lm);
+                const int l = lofm[lm];
                 R uu = 0, ww = 0;
                 dot2(hs + (s * L2 + lm) * NMP, Ism + (t * L + l) * NMP, dIsm + (t * L + l) * NMP, NMP, uu, ww);
                 const Dual<R> y = Yd[t * L2 + lm];
@@ -604,16 +706,27 @@ __global__ void k_iota(int n, int* out) {
 
 template <class R>
 size_t fwd_smem(const SoapConst& sc) {
-    const int L = sc.l_max + 1, L2 = L * L, NMP = nmp_of(sc.n_max), NS = sc.n_species;
-    const size_t stage = (size_t)TC * L2 + (size_t)TC * L * NMP + TC + TC * DS;
-    const size_t ps = (size_t)sc.n_pairs * L;
-    return sizeof(R) * ((size_t)soap_tab(sc.n_max, L).size + (size_t)NS * L2 * NMP + (size_t)NS * sc.n_max * L2 +
-                        std::max(stage, ps)) +
-           sizeof(int) * (TC + NS * TC + NS) + 64;
+    const int L = sc.l_max + 1, L2 = L * L, NS = sc.n_species;
+    return sizeof(R) * ((size_t)soap_tab(sc.n_max, L).size + (size_t)((NS * sc.n_max * L2 + 3) & ~3) + fwd_region(sc)) +
+           sizeof(int) * (TC + NS * TC + NS) + (size_t)L2 + 64;
 }
 template <class R>
 size_t bwd_smem(const SoapConst& sc) {
-    return sizeof(R) * (size_t)bwd_plan(sc).ints_at + sizeof(int) * (TCB + sc.n_species * TCB + sc.n_species) + 64;
+    const int L = sc.l_max + 1;
+    return sizeof(R) * (size_t)bwd_plan(sc).ints_at + sizeof(int) * (TCB + sc.n_species * TCB + sc.n_species) +
+           (size_t)(L * L) + 64;
+}
+
+template <class R, int FQ>
+int launch_forward_fq(gapgpu_context& c, const Coordinate& co, int nc, const SoapConst& sc, size_t sm) {
+    GG_CUDA(cudaFuncSetAttribute(k_soap_forward<R, FQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const R* tab = static_cast<const R*>(co.dtab[sizeof(R) == 4 ? 1 : 0]);
+    k_soap_forward<R, FQ><<<nc, FWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.cur_centres, c.Z.as<int>(), c.nbr_off.as<int>(),
+                                                             c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.scratch.as<R>(),
+                                                             c.qbuf.as<R>(), c.pnorm.as<double>());
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
 }
 
 template <class R>
@@ -621,14 +734,10 @@ int launch_forward(gapgpu_context& c, const Coordinate& co, int nc) {
     SoapConst sc = soap_const(co);
     size_t sm = fwd_smem<R>(sc);
     if (sm > 200 * 1024) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the shared-memory forward kernel");
-    GG_CUDA(cudaFuncSetAttribute(k_soap_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    const R* tab = static_cast<const R*>(co.dtab[sizeof(R) == 4 ? 1 : 0]);
-    k_soap_forward<R><<<nc, FWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.cur_centres, c.Z.as<int>(),
-                                                         c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(),
-                                                         c.scratch.as<R>(), c.qbuf.as<R>(), c.pnorm.as<double>());
-    c.launches++;
-    GG_CUDA(cudaGetLastError());
-    return GAPGPU_OK;
+    const int items = sc.n_species * (sc.l_max + 1) * (sc.l_max + 1) * (nmp_of(sc.n_max) / 4);
+    if (items <= FQ_SMALL * FWD_THREADS) return launch_forward_fq<R, FQ_SMALL>(c, co, nc, sc, sm);
+    if (items <= FQ_LARGE * FWD_THREADS) return launch_forward_fq<R, FQ_LARGE>(c, co, nc, sc, sm);
+    GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the forward kernel's register accumulators");
 }
 
 template <class R>
