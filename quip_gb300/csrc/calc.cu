@@ -116,7 +116,7 @@ constexpr int RED_CHUNK = 4096;  // atoms per first-level reduction block (relat
 // list is kept), per-coordinate centre lists, segmented-reduction tables and the
 // output buffers.  All host synchronisation of an evaluation happens here.
 int prepare(gapgpu_context& c, int nstruct, const int* n_atoms, const double* lattices, const int* pbcs, const int* d_mask,
-            double cutoff, bool rebuild) {
+            double cutoff, bool rebuild, int precision) {
     const gapgpu_model& m = *c.model;
     int rc, n = 0;
     for (int s = 0; s < nstruct; ++s) n += n_atoms[s];
@@ -128,7 +128,8 @@ int prepare(gapgpu_context& c, int nstruct, const int* n_atoms, const double* la
         cudaEventRecord(c.nev[0], c.stream);
     }
     if (rebuild) {
-        if ((rc = build_neighbours_batch(c, nstruct, n_atoms, d_pos, lattices, pbcs, cutoff))) return rc;
+        if ((rc = build_neighbours_batch(c, nstruct, n_atoms, d_pos, lattices, pbcs, cutoff, precision != GAPGPU_FP64)))
+            return rc;
     } else {
         if (n != c.n_total || nstruct != c.nstruct) GG_FAIL(GAPGPU_ERR_ARG, "kept neighbour list does not match the atoms");
         if ((rc = refresh_distances(c, d_pos))) return rc;
@@ -500,7 +501,7 @@ int gapgpu_calc(gapgpu_context* c, int n, const double* pos, const int32_t* Z, c
     }
     if ((rc = copy_inputs(*c, n, pos, Z, atom_mask, cudaMemcpyHostToDevice))) return rc;
     const int* dmask = atom_mask ? c->mask.as<int>() : nullptr;
-    if ((rc = prepare(*c, 1, &n, lattice, pbc, dmask, c->model->cutoff, true))) return rc;
+    if ((rc = prepare(*c, 1, &n, lattice, pbc, dmask, c->model->cutoff, true, prec))) return rc;
     if ((rc = run_evaluation(*c, prec, dmask))) return rc;
     double red[10];
     GG_CUDA(cudaMemcpyAsync(red, c->out_e.p, sizeof red, cudaMemcpyDeviceToHost, c->stream));
@@ -521,7 +522,7 @@ int gapgpu_calc_device(gapgpu_context* c, int n, const double* d_pos, const int3
     c->launches = 0;
     int rc;
     if ((rc = copy_inputs(*c, n, d_pos, d_Z, nullptr, cudaMemcpyDeviceToDevice))) return rc;
-    if ((rc = prepare(*c, 1, &n, lattice, pbc, nullptr, c->model->cutoff, true))) return rc;
+    if ((rc = prepare(*c, 1, &n, lattice, pbc, nullptr, c->model->cutoff, true, c->precision))) return rc;
     if ((rc = run_evaluation(*c, c->precision, nullptr))) return rc;
     if (d_energy) GG_CUDA(cudaMemcpyAsync(d_energy, c->out_e.p, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     if (d_virial)
@@ -547,7 +548,7 @@ int gapgpu_calc_batch(gapgpu_context* c, int nstruct, const int32_t* n_atoms, co
     if (n > (1LL << 30)) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_batch: too many atoms");
     if (n > 0 && (!pos || !Z)) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_batch: NULL positions or species");
     if ((rc = copy_inputs(*c, (int)n, pos, Z, nullptr, cudaMemcpyHostToDevice))) return rc;
-    if ((rc = prepare(*c, nstruct, n_atoms, lattices, pbcs, nullptr, c->model->cutoff, true))) return rc;
+    if ((rc = prepare(*c, nstruct, n_atoms, lattices, pbcs, nullptr, c->model->cutoff, true, prec))) return rc;
     if ((rc = run_evaluation(*c, prec, nullptr))) return rc;
     std::vector<double> red(10 * (size_t)nstruct);
     GG_CUDA(cudaMemcpyAsync(red.data(), c->out_e.p, sizeof(double) * red.size(), cudaMemcpyDeviceToHost, c->stream));

@@ -28,7 +28,8 @@ struct GeomDev {
     double lat[9], lat_eff_inv[9], lat_off[3], cutoff;
     double origin[3];     // Cartesian corner of the effective cell (non-periodic axes)
     double ginv[9];       // inverse of the true lattice
-    float lat32[9];
+    float lat32[9];       // FP32 lattice (hi part)
+    float lat_lo[9];      // lattice - lat32 (lo part), for the mixed path's displacements
     float lim2;           // (cutoff + margin)^2: FP32 distances above it are certainly outside
     float sure2;          // (cutoff - margin)^2: FP32 distances below it are certainly inside
     int cellsN[3], img[3], pbc[3];
@@ -49,7 +50,8 @@ struct gapgpu_context {
     gapgpu::DBuf pos, Z, mask, out_e, out_f, out_v, out_le, out_lv;
     // cells and neighbours
     gapgpu::DBuf cell_key, cell_key2, atom_idx, atom_idx2, cell_start, cell_end, ms, cub_tmp, minmax;
-    gapgpu::DBuf nbr_cnt, nbr_off, nbr_j, nbr_d, nbr_s, nbr_rev, nbr_i, wpos, total, geoms, sid, dispmax;
+    gapgpu::DBuf nbr_cnt, nbr_off, nbr_j, nbr_d, nbr_s, nbr_rev, nbr_i, wpos, total, geoms, sid, dispmax, phi, plo;
+    bool nbr_mixed = false;  // displacements of the last build in FP32 error-free arithmetic (mixed path)
     std::vector<gapgpu::GeomDev> h_geoms;  // geometry of the structures of the last neighbour build
     int n_atoms_built = 0;
     // per pair / per atom accumulators
@@ -79,7 +81,7 @@ struct gapgpu_context {
     std::vector<gapgpu::DBuf*> buffers() {
         return {&pos, &Z, &mask, &out_e, &out_f, &out_v, &out_le, &out_lv, &cell_key, &cell_key2, &atom_idx, &atom_idx2,
                 &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev,
-                &nbr_i, &wpos, &total, &geoms, &sid, &dispmax, &fpair, &epair, &eatom, &redpart, &flags, &centres,
+                &nbr_i, &wpos, &total, &geoms, &sid, &dispmax, &phi, &plo, &fpair, &epair, &eatom, &redpart, &flags, &centres,
                 &ncent, &coef, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf, &Wlo, &epart, &ecent, &Gbuf, &scratch, &chunks, &schunk};
     }
     std::vector<const gapgpu::DBuf*> buffers() const {
@@ -94,12 +96,12 @@ namespace gapgpu {
 int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double* lattice, const int* pbc, double cutoff,
                      const int* d_Z_for_check);
 int build_neighbours_batch(gapgpu_context& c, int nstruct, const int* n_atoms, const double* d_pos, const double* lattices,
-                           const int* pbcs, double cutoff);
+                           const int* pbcs, double cutoff, bool mixed = false);
 int refresh_distances(gapgpu_context& c, const double* d_pos);
 int max_displacement(gapgpu_context& c, const double* d_pos, const double* d_ref, int n, double* out);
 // calc.cu
 int prepare(gapgpu_context& c, int nstruct, const int* n_atoms, const double* lattices, const int* pbcs, const int* d_mask,
-            double cutoff, bool rebuild);
+            double cutoff, bool rebuild, int precision);
 int run_evaluation(gapgpu_context& c, int precision, const int* d_mask);
 int check_device_flags(gapgpu_context& c);
 // soap.cu

@@ -59,6 +59,58 @@ __device__ __forceinline__ void pair_vector(const double* __restrict__ pos, cons
     r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
 }
 
+// Error-free transformations (Knuth's TwoSum; TwoProd with a fused multiply-add),
+// written with round-to-nearest intrinsics so that the compiler neither fuses nor
+// reorders them.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// One component of d = pos_b - pos_a + L s in FP32, each position and lattice entry
+// carried as hi + lo floats: the large terms are summed exactly (TwoSum/TwoProd) and
+// the small ones added to the error, so d is accurate to about one FP32 ulp of |d|
+// even when the positions are far from the origin.
+__device__ __forceinline__ float eft_component(float bh, float bl, float ah, float al, const float* Lh, const float* Ll,
+                                               float s0, float s1, float s2) {
+    float hi, e, err;
+    two_sum(bh, -ah, hi, err);
+    const float sk[3] = {s0, s1, s2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float p = __fmul_rn(Lh[3 * k], sk[k]);
+        const float ep = __fmaf_rn(Lh[3 * k], sk[k], -p);
+        two_sum(hi, p, hi, e);
+        err += e + ep + Ll[3 * k] * sk[k];
+    }
+    return hi + (err + (bl - al));
+}
+
+__device__ __forceinline__ void pair_vector_mixed(const float4* __restrict__ phi, const float4* __restrict__ plo,
+                                                  const GeomDev& g, int a, int b, int s0, int s1, int s2, double& d0,
+                                                  double& d1, double& d2, double& r) {
+    const float4 ah = phi[a], al = plo[a], bh = phi[b], bl = plo[b];
+    const float f0 = (float)s0, f1 = (float)s1, f2 = (float)s2;
+    const float x = eft_component(bh.x, bl.x, ah.x, al.x, g.lat32, g.lat_lo, f0, f1, f2);
+    const float y = eft_component(bh.y, bl.y, ah.y, al.y, g.lat32 + 1, g.lat_lo + 1, f0, f1, f2);
+    const float z = eft_component(bh.z, bl.z, ah.z, al.z, g.lat32 + 2, g.lat_lo + 2, f0, f1, f2);
+    d0 = x;
+    d1 = y;
+    d2 = z;
+    r = sqrtf(x * x + y * y + z * z);
+}
+
+// Positions as hi + lo floats for the mixed path's displacements.
+__global__ void k_split_pos(int n, const double* __restrict__ pos, float4* __restrict__ phi, float4* __restrict__ plo) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const double x = pos[3 * a], y = pos[3 * a + 1], z = pos[3 * a + 2];
+    const float hx = (float)x, hy = (float)y, hz = (float)z;
+    phi[a] = make_float4(hx, hy, hz, 0.f);
+    plo[a] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), 0.f);
+}
+
 __global__ void k_assign(int n, const double* __restrict__ pos, const GeomDev* __restrict__ geoms,
                          const int* __restrict__ sid, int* __restrict__ key, int* __restrict__ idx, int* __restrict__ ms,
                          int* __restrict__ bad) {
@@ -115,8 +167,11 @@ __global__ void k_cell_ranges(int n, const int* __restrict__ key, int* __restric
 // decisions; the fill pass computes the FP64 displacement of every kept pair.
 // CALLER_LAYOUT (fill only): write just j and the unpacked shift (3 ints per entry)
 // into caller-owned arrays, the layout of gapgpu_neighbours; nd/ni are not written.
-template <bool FILL, bool CALLER_LAYOUT = false>
+// MIXED (fill only): kept pairs outside the band take their displacement from the FP32
+// error-free arithmetic of pair_vector_mixed instead of FP64.
+template <bool FILL, bool CALLER_LAYOUT = false, bool MIXED = false>
 __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__ pos, const float4* __restrict__ wpos,
+                                               const float4* __restrict__ phi, const float4* __restrict__ plo,
                                                const GeomDev* __restrict__ geoms, const int* __restrict__ sid,
                                                const int* __restrict__ key_of_atom, const int* __restrict__ ms,
                                                const int* __restrict__ sorted, const int* __restrict__ cstart,
@@ -180,8 +235,13 @@ __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__
                         if (!FILL && sure && !self0) keep = true;
                         else if (!self0 && r2 < lim2) {
                             s0 = i4 - msa0 + ms[3 * b]; s1 = j4 - msa1 + ms[3 * b + 1]; s2 = k4 - msa2 + ms[3 * b + 2];
-                            pair_vector(pos, g.lat, a, b, s0, s1, s2, d0, d1, d2, r);
-                            keep = sure || (!(d0 > cutoff || d1 > cutoff || d2 > cutoff) && r < cutoff);
+                            if (MIXED && sure) {
+                                pair_vector_mixed(phi, plo, g, a, b, s0, s1, s2, d0, d1, d2, r);
+                                keep = true;
+                            } else {
+                                pair_vector(pos, g.lat, a, b, s0, s1, s2, d0, d1, d2, r);
+                                keep = sure || (!(d0 > cutoff || d1 > cutoff || d2 > cutoff) && r < cutoff);
+                            }
                         }
                     }
                     const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -223,15 +283,19 @@ __global__ void k_reverse(long long P, const int* __restrict__ off, const int* _
 
 // connection_calc_dists: new displacements for an existing list (same formula as the
 // fill pass, so a refreshed list equals a rebuilt one entry for entry).
-__global__ void k_distances(long long P, const double* __restrict__ pos, const GeomDev* __restrict__ geoms,
-                            const int* __restrict__ sid, const int* __restrict__ ni, const int* __restrict__ nj,
-                            const int* __restrict__ ns, double4* __restrict__ nd, int* __restrict__ bad) {
+template <bool MIXED>
+__global__ void k_distances(long long P, const double* __restrict__ pos, const float4* __restrict__ phi,
+                            const float4* __restrict__ plo, const GeomDev* __restrict__ geoms, const int* __restrict__ sid,
+                            const int* __restrict__ ni, const int* __restrict__ nj, const int* __restrict__ ns,
+                            double4* __restrict__ nd, int* __restrict__ bad) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (p >= P) return;
     const int a = ni[p], b = nj[p], s = ns[p];
     const GeomDev& g = geoms[sid_of(sid, a)];
     double d0, d1, d2, r;
-    pair_vector(pos, g.lat, a, b, (s & 1023) - 512, ((s >> 10) & 1023) - 512, ((s >> 20) & 1023) - 512, d0, d1, d2, r);
+    const int s0 = (s & 1023) - 512, s1 = ((s >> 10) & 1023) - 512, s2 = ((s >> 20) & 1023) - 512;
+    if (MIXED) pair_vector_mixed(phi, plo, g, a, b, s0, s1, s2, d0, d1, d2, r);
+    else pair_vector(pos, g.lat, a, b, s0, s1, s2, d0, d1, d2, r);
     nd[p] = make_double4(d0, d1, d2, r);
     if (r < 1e-10) atomicOr(bad, 2);
 }
@@ -390,7 +454,10 @@ int geom_finish(GeomDev& g, int n, const double* mm) {
             g.origin[d] = lat_eff[d] * g.lat_off[0] + lat_eff[3 + d] * g.lat_off[1] + lat_eff[6 + d] * g.lat_off[2];
             bsize += norm3(lat_eff + 3 * d);
         }
-        for (int k = 0; k < 9; ++k) g.lat32[k] = (float)lattice[k];
+        for (int k = 0; k < 9; ++k) {
+            g.lat32[k] = (float)lattice[k];
+            g.lat_lo[k] = (float)(lattice[k] - (double)g.lat32[k]);
+        }
         double margin = 1e-3 + 1e-6 * bsize + 1e-6 * cutoff;
         g.lim2 = (float)((cutoff + margin) * (cutoff + margin));
         g.sure2 = cutoff > margin ? (float)((cutoff - margin) * (cutoff - margin)) : 0.0f;
@@ -419,7 +486,7 @@ void DBuf::release() {
 }
 
 int build_neighbours_batch(gapgpu_context& c, int nstruct, const int* n_atoms, const double* d_pos, const double* lattices,
-                           const int* pbcs, double cutoff) {
+                           const int* pbcs, double cutoff, bool mixed) {
     cudaStream_t st = c.stream;
     if (nstruct < 1) GG_FAIL(GAPGPU_ERR_ARG, "neighbour build: no structures");
     std::vector<GeomDev>& hg = c.h_geoms;
@@ -473,10 +540,16 @@ int build_neighbours_batch(gapgpu_context& c, int nstruct, const int* n_atoms, c
         (rc = c.ms.ensure(sizeof(int) * 3 * n)) || (rc = c.cell_start.ensure(sizeof(int) * ncell)) ||
         (rc = c.cell_end.ensure(sizeof(int) * ncell)) || (rc = c.nbr_cnt.ensure(sizeof(int) * (n + 1))) ||
         (rc = c.nbr_off.ensure(sizeof(int) * (n + 1))) || (rc = c.total.ensure(sizeof(int) * 4)) ||
-        (rc = c.wpos.ensure(sizeof(float4) * n)))
+        (rc = c.wpos.ensure(sizeof(float4) * n)) || (rc = c.phi.ensure(sizeof(float4) * n)) ||
+        (rc = c.plo.ensure(sizeof(float4) * n)))
         return rc;
+    c.nbr_mixed = mixed;
     int* bad = c.total.as<int>() + 2;
     GG_CUDA(cudaMemsetAsync(c.total.p, 0, sizeof(int) * 4, st));
+    if (mixed) {
+        k_split_pos<<<(n + 255) / 256, 256, 0, st>>>(n, d_pos, c.phi.as<float4>(), c.plo.as<float4>());
+        c.launches++;
+    }
     const int TB = 128, nb = (n + TB - 1) / TB;
     const int nbw = (int)(((long long)n * 32 + TB - 1) / TB);  // one warp per atom
     k_assign<<<nb, TB, 0, st>>>(n, d_pos, dg, sid, c.cell_key.as<int>(), c.atom_idx.as<int>(), c.ms.as<int>(), bad);
@@ -495,8 +568,8 @@ int build_neighbours_batch(gapgpu_context& c, int nstruct, const int* n_atoms, c
     GG_CUDA(cudaMemsetAsync(c.cell_end.p, 0, sizeof(int) * ncell, st));
     k_cell_ranges<<<nb, TB, 0, st>>>(n, c.cell_key2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>());
     k_wrapped<<<nb, TB, 0, st>>>(n, d_pos, dg, sid, c.atom_idx2.as<int>(), c.ms.as<int>(), c.wpos.as<float4>());
-    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), dg, sid, c.cell_key.as<int>(), c.ms.as<int>(),
-                                       c.atom_idx2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>(),
+    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), nullptr, nullptr, dg, sid, c.cell_key.as<int>(),
+                                       c.ms.as<int>(), c.atom_idx2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>(),
                                        c.nbr_cnt.as<int>(), nullptr, nullptr, nullptr, nullptr, nullptr, bad);
     GG_CUDA(cudaMemsetAsync(c.nbr_cnt.as<int>() + n, 0, sizeof(int), st));
     GG_CUDA(cub::DeviceScan::ExclusiveSum(c.cub_tmp.p, tmp2, c.nbr_cnt.as<int>(), c.nbr_off.as<int>(), n + 1, st));
@@ -511,10 +584,16 @@ int build_neighbours_batch(gapgpu_context& c, int nstruct, const int* n_atoms, c
         (rc = c.nbr_s.ensure(sizeof(int) * P)) || (rc = c.nbr_rev.ensure(sizeof(int) * P)) ||
         (rc = c.nbr_i.ensure(sizeof(int) * P)))
         return rc;
-    k_pairs<true><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), dg, sid, c.cell_key.as<int>(), c.ms.as<int>(),
-                                      c.atom_idx2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>(), nullptr,
-                                      c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.nbr_s.as<int>(),
-                                      c.nbr_i.as<int>(), bad);
+    if (mixed)
+        k_pairs<true, false, true><<<nbw, TB, 0, st>>>(
+            n, d_pos, c.wpos.as<float4>(), c.phi.as<float4>(), c.plo.as<float4>(), dg, sid, c.cell_key.as<int>(),
+            c.ms.as<int>(), c.atom_idx2.as<int>(), c.cell_start.as<int>(), c.cell_end.as<int>(), nullptr,
+            c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.nbr_s.as<int>(), c.nbr_i.as<int>(), bad);
+    else
+        k_pairs<true><<<nbw, TB, 0, st>>>(n, d_pos, c.wpos.as<float4>(), nullptr, nullptr, dg, sid, c.cell_key.as<int>(),
+                                          c.ms.as<int>(), c.atom_idx2.as<int>(), c.cell_start.as<int>(),
+                                          c.cell_end.as<int>(), nullptr, c.nbr_off.as<int>(), c.nbr_j.as<int>(),
+                                          c.nbr_d.as<double4>(), c.nbr_s.as<int>(), c.nbr_i.as<int>(), bad);
     if (tot > 0)
         k_reverse<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(tot, c.nbr_off.as<int>(), c.nbr_j.as<int>(),
                                                                   c.nbr_i.as<int>(), c.nbr_s.as<int>(), c.nbr_rev.as<int>(),
@@ -538,10 +617,21 @@ int refresh_distances(gapgpu_context& c, const double* d_pos) {
     const long long P = c.n_pairs;
     if (P == 0) return GAPGPU_OK;
     int* bad = c.total.as<int>() + 2;
-    k_distances<<<(unsigned)((P + 255) / 256), 256, 0, c.stream>>>(
-        P, d_pos, c.geoms.as<GeomDev>(), c.h_geoms.size() > 1 ? c.sid.as<int>() : nullptr, c.nbr_i.as<int>(),
-        c.nbr_j.as<int>(), c.nbr_s.as<int>(), c.nbr_d.as<double4>(), bad);
-    c.launches++;
+    const int* sid = c.h_geoms.size() > 1 ? c.sid.as<int>() : nullptr;
+    const unsigned nb = (unsigned)((P + 255) / 256);
+    if (c.nbr_mixed) {
+        const int n = c.n_atoms_built;
+        k_split_pos<<<(n + 255) / 256, 256, 0, c.stream>>>(n, d_pos, c.phi.as<float4>(), c.plo.as<float4>());
+        k_distances<true><<<nb, 256, 0, c.stream>>>(P, d_pos, c.phi.as<float4>(), c.plo.as<float4>(), c.geoms.as<GeomDev>(),
+                                                    sid, c.nbr_i.as<int>(), c.nbr_j.as<int>(), c.nbr_s.as<int>(),
+                                                    c.nbr_d.as<double4>(), bad);
+        c.launches += 2;
+    } else {
+        k_distances<false><<<nb, 256, 0, c.stream>>>(P, d_pos, nullptr, nullptr, c.geoms.as<GeomDev>(), sid,
+                                                     c.nbr_i.as<int>(), c.nbr_j.as<int>(), c.nbr_s.as<int>(),
+                                                     c.nbr_d.as<double4>(), bad);
+        c.launches++;
+    }
     GG_CUDA(cudaGetLastError());
     return GAPGPU_OK;
 }
@@ -691,8 +781,8 @@ extern "C" int gapgpu_neighbours_static(int n, const double* d_pos, const double
     GG_CUDA(cub::DeviceRadixSort::SortPairs(cub_tmp, t_sort, key, key2, idx, idx2, n, 0, endbit, st));
     k_cell_ranges<<<nb, TB, 0, st>>>(n, key2, cstart, cend);
     k_wrapped<<<nb, TB, 0, st>>>(n, d_pos, dg, nullptr, idx2, ms, wpos);
-    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, wpos, dg, nullptr, key, ms, idx2, cstart, cend, cnt, nullptr, nullptr,
-                                       nullptr, nullptr, nullptr, bad);
+    k_pairs<false><<<nbw, TB, 0, st>>>(n, d_pos, wpos, nullptr, nullptr, dg, nullptr, key, ms, idx2, cstart, cend, cnt,
+                                       nullptr, nullptr, nullptr, nullptr, nullptr, bad);
     GG_CUDA(cub::DeviceScan::ExclusiveSum(cub_tmp, t_scan, cnt, d_offsets, n + 1, st));
     int tot = 0;
     GG_CUDA(cudaMemcpyAsync(&tot, d_offsets + n, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -700,8 +790,8 @@ extern "C" int gapgpu_neighbours_static(int n, const double* d_pos, const double
     if (tot < 0) GG_FAIL(GAPGPU_ERR_ATOMS, "neighbour list larger than 2^31 entries");
     *total = tot;
     if (tot > 0 && capacity >= tot && d_nbr_j && d_nbr_shift)
-        k_pairs<true, true><<<nbw, TB, 0, st>>>(n, d_pos, wpos, dg, nullptr, key, ms, idx2, cstart, cend, nullptr, d_offsets,
-                                                d_nbr_j, nullptr, d_nbr_shift, nullptr, bad);
+        k_pairs<true, true><<<nbw, TB, 0, st>>>(n, d_pos, wpos, nullptr, nullptr, dg, nullptr, key, ms, idx2, cstart, cend,
+                                                nullptr, d_offsets, d_nbr_j, nullptr, d_nbr_shift, nullptr, bad);
     int flags = 0;
     GG_CUDA(cudaMemcpyAsync(&flags, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     GG_CUDA(cudaStreamSynchronize(st));
