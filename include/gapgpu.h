@@ -159,6 +159,19 @@ int gapgpu_selftest_bounded_wait(gapgpu_context* ctx, int64_t limit);
 /* Wait for the context's stream. */
 int gapgpu_context_sync(gapgpu_context* ctx);
 
+/* LAMMPS pair_style quip path: quip_lammps_wrapper (src/Potentials/quip_lammps_wrapper.f95:
+ * 30-156) with the host's own neighbour list and explicit ghost atoms (no periodic
+ * shifts; `lattice` only enters the virial's bookkeeping).  nlocal + nghost atoms with
+ * Z and pos double[3*(nlocal+nghost)]; ilist[inum] (0-based) lists the local atoms,
+ * which are the only centres (atom_mask_name=local); num_neigh[inum] and neigh (packed,
+ * 1-based, as the wrapper reads them) give each local atom's FULL neighbour list.
+ * Outputs (nullable) have the wrapper's shapes: energy, local_e[n], virial[9],
+ * local_virial[9n], force[3n] including the forces on ghosts, which the host sums back
+ * onto their owners.  Uses the context's precision. */
+int gapgpu_calc_lammps(gapgpu_context* ctx, int nlocal, int nghost, const int32_t* Z, int inum, const int32_t* ilist,
+                       const int32_t* num_neigh, const int32_t* neigh, const double* lattice, const double* pos,
+                       double* energy, double* local_e, double* virial, double* local_virial, double* force);
+
 /* Neighbour list with QUIP semantics (no minimum image, every periodic image within
  * `cutoff`, strict r < cutoff) built on the GPU: connection_calc_connect
  * (Connection.f95:1035-1310).  Returns per-atom CSR (offsets n+1, j, shift 3 per

@@ -112,11 +112,13 @@ constexpr int RED_CHUNK = 4096;  // atoms per first-level reduction block (relat
 }
 
 // ---------------------------------------------------------------- phase A
-// Neighbour list (rebuilt at `cutoff`, or only its displacements refreshed when the
-// list is kept), per-coordinate centre lists, segmented-reduction tables and the
-// output buffers.  All host synchronisation of an evaluation happens here.
+// Neighbour list (rebuilt at `cutoff`, only its displacements refreshed when the list
+// is kept, or already loaded from the caller), per-coordinate centre lists,
+// segmented-reduction tables and the output buffers.  All host synchronisation of an
+// evaluation happens here.
 int prepare(gapgpu_context& c, int nstruct, const int* n_atoms, const double* lattices, const int* pbcs, const int* d_mask,
-            double cutoff, bool rebuild, int precision) {
+            double cutoff, int list_mode, int precision) {
+    const bool rebuild = list_mode != LIST_REFRESH;
     const gapgpu_model& m = *c.model;
     int rc, n = 0;
     for (int s = 0; s < nstruct; ++s) n += n_atoms[s];
@@ -127,10 +129,10 @@ int prepare(gapgpu_context& c, int nstruct, const int* n_atoms, const double* la
             if (!e) cudaEventCreate(&e);
         cudaEventRecord(c.nev[0], c.stream);
     }
-    if (rebuild) {
+    if (list_mode == LIST_BUILD) {
         if ((rc = build_neighbours_batch(c, nstruct, n_atoms, d_pos, lattices, pbcs, cutoff, precision != GAPGPU_FP64)))
             return rc;
-    } else {
+    } else if (list_mode == LIST_REFRESH) {
         if (n != c.n_total || nstruct != c.nstruct) GG_FAIL(GAPGPU_ERR_ARG, "kept neighbour list does not match the atoms");
         if ((rc = refresh_distances(c, d_pos))) return rc;
     }
@@ -501,7 +503,7 @@ int gapgpu_calc(gapgpu_context* c, int n, const double* pos, const int32_t* Z, c
     }
     if ((rc = copy_inputs(*c, n, pos, Z, atom_mask, cudaMemcpyHostToDevice))) return rc;
     const int* dmask = atom_mask ? c->mask.as<int>() : nullptr;
-    if ((rc = prepare(*c, 1, &n, lattice, pbc, dmask, c->model->cutoff, true, prec))) return rc;
+    if ((rc = prepare(*c, 1, &n, lattice, pbc, dmask, c->model->cutoff, LIST_BUILD, prec))) return rc;
     if ((rc = run_evaluation(*c, prec, dmask))) return rc;
     double red[10];
     GG_CUDA(cudaMemcpyAsync(red, c->out_e.p, sizeof red, cudaMemcpyDeviceToHost, c->stream));
@@ -522,7 +524,7 @@ int gapgpu_calc_device(gapgpu_context* c, int n, const double* d_pos, const int3
     c->launches = 0;
     int rc;
     if ((rc = copy_inputs(*c, n, d_pos, d_Z, nullptr, cudaMemcpyDeviceToDevice))) return rc;
-    if ((rc = prepare(*c, 1, &n, lattice, pbc, nullptr, c->model->cutoff, true, c->precision))) return rc;
+    if ((rc = prepare(*c, 1, &n, lattice, pbc, nullptr, c->model->cutoff, LIST_BUILD, c->precision))) return rc;
     if ((rc = run_evaluation(*c, c->precision, nullptr))) return rc;
     if (d_energy) GG_CUDA(cudaMemcpyAsync(d_energy, c->out_e.p, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     if (d_virial)
@@ -548,7 +550,7 @@ int gapgpu_calc_batch(gapgpu_context* c, int nstruct, const int32_t* n_atoms, co
     if (n > (1LL << 30)) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_batch: too many atoms");
     if (n > 0 && (!pos || !Z)) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_batch: NULL positions or species");
     if ((rc = copy_inputs(*c, (int)n, pos, Z, nullptr, cudaMemcpyHostToDevice))) return rc;
-    if ((rc = prepare(*c, nstruct, n_atoms, lattices, pbcs, nullptr, c->model->cutoff, true, prec))) return rc;
+    if ((rc = prepare(*c, nstruct, n_atoms, lattices, pbcs, nullptr, c->model->cutoff, LIST_BUILD, prec))) return rc;
     if ((rc = run_evaluation(*c, prec, nullptr))) return rc;
     std::vector<double> red(10 * (size_t)nstruct);
     GG_CUDA(cudaMemcpyAsync(red.data(), c->out_e.p, sizeof(double) * red.size(), cudaMemcpyDeviceToHost, c->stream));
@@ -560,6 +562,69 @@ int gapgpu_calc_batch(gapgpu_context* c, int nstruct, const int32_t* n_atoms, co
         if (energies) energies[s] = red[10 * (size_t)s];
         if (virials) std::memcpy(virials + 9 * (size_t)s, &red[10 * (size_t)s + 1], 9 * sizeof(double));
     }
+    return GAPGPU_OK;
+}
+
+int gapgpu_calc_lammps(gapgpu_context* c, int nlocal, int nghost, const int32_t* Z, int inum, const int32_t* ilist,
+                       const int32_t* num_neigh, const int32_t* neigh, const double* lattice, const double* pos,
+                       double* energy, double* local_e, double* virial, double* local_virial, double* force) {
+    if (!c || nlocal < 0 || nghost < 0 || inum < 0 || !lattice || (nlocal + nghost > 0 && (!Z || !pos)) ||
+        (inum > 0 && (!ilist || !num_neigh)))
+        GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_lammps: bad argument");
+    c->launches = 0;
+    const int n = nlocal + nghost;
+    if (nlocal == 0) {  // an empty region: every output zero, as the reference wrapper does
+        if (energy) *energy = 0;
+        if (virial) std::memset(virial, 0, 9 * sizeof(double));
+        if (local_e) std::memset(local_e, 0, sizeof(double) * n);
+        if (local_virial) std::memset(local_virial, 0, 9 * sizeof(double) * n);
+        if (force) std::memset(force, 0, 3 * sizeof(double) * n);
+        return GAPGPU_OK;
+    }
+    // the local atoms are the centres; the full per-local-atom lists are completed with
+    // the ghost -> local entries so that ghosts receive their forces by the same gather
+    std::vector<int32_t> local(n, 0);
+    for (int k = 0; k < inum; ++k) {
+        if (ilist[k] < 0 || ilist[k] >= n) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_lammps: ilist entry out of range");
+        local[ilist[k]] = 1;
+    }
+    std::vector<int> cnt(n + 1, 0);
+    long long total = 0;
+    for (int k = 0; k < inum; ++k) total += num_neigh[k];
+    if (total > 0 && !neigh) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_lammps: NULL neighbour list");
+    for (long long q = 0, k = 0; k < inum; ++k)
+        for (int m = 0; m < num_neigh[k]; ++m, ++q) {
+            const int i = ilist[k], j = neigh[q] - 1;  // neighbours are 1-based, as quip_lammps_wrapper reads them
+            if (j < 0 || j >= n || j == i) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_lammps: neighbour index out of range");
+            cnt[i + 1]++;
+            if (!local[j]) cnt[j + 1]++;
+        }
+    for (int a = 0; a < n; ++a) cnt[a + 1] += cnt[a];
+    std::vector<int> off(cnt), nj(cnt[n]), fill(cnt.begin(), cnt.end() - 1);
+    for (long long q = 0, k = 0; k < inum; ++k)
+        for (int m = 0; m < num_neigh[k]; ++m, ++q) {
+            const int i = ilist[k], j = neigh[q] - 1;
+            nj[fill[i]++] = j;
+            if (!local[j]) nj[fill[j]++] = i;
+        }
+    int rc;
+    if ((rc = copy_inputs(*c, n, pos, Z, local.data(), cudaMemcpyHostToDevice))) return rc;
+    const int* dmask = c->mask.as<int>();
+    const int prec = c->precision;
+    if ((rc = load_external_neighbours(*c, n, off, nj, lattice, prec != GAPGPU_FP64))) return rc;
+    const int pbc[3] = {0, 0, 0};
+    if ((rc = prepare(*c, 1, &n, lattice, pbc, dmask, c->model->cutoff, LIST_GIVEN, prec))) return rc;
+    if ((rc = run_evaluation(*c, prec, dmask))) return rc;
+    double red[10];
+    GG_CUDA(cudaMemcpyAsync(red, c->out_e.p, sizeof red, cudaMemcpyDeviceToHost, c->stream));
+    if (force) GG_CUDA(cudaMemcpyAsync(force, c->out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    if (local_e) GG_CUDA(cudaMemcpyAsync(local_e, c->out_le.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (local_virial)
+        GG_CUDA(cudaMemcpyAsync(local_virial, c->out_lv.p, sizeof(double) * 9 * n, cudaMemcpyDeviceToHost, c->stream));
+    GG_CUDA(cudaStreamSynchronize(c->stream));
+    if ((rc = check_device_flags(*c))) return rc;
+    if (energy) *energy = red[0];
+    if (virial) std::memcpy(virial, red + 1, 9 * sizeof(double));
     return GAPGPU_OK;
 }
 

@@ -98,10 +98,13 @@ int build_neighbours(gapgpu_context& c, int n, const double* d_pos, const double
 int build_neighbours_batch(gapgpu_context& c, int nstruct, const int* n_atoms, const double* d_pos, const double* lattices,
                            const int* pbcs, double cutoff, bool mixed = false);
 int refresh_distances(gapgpu_context& c, const double* d_pos);
+int load_external_neighbours(gapgpu_context& c, int n, const std::vector<int>& off, const std::vector<int>& nj,
+                             const double* lattice, bool mixed);
 int max_displacement(gapgpu_context& c, const double* d_pos, const double* d_ref, int n, double* out);
 // calc.cu
+enum ListMode { LIST_BUILD = 0, LIST_REFRESH = 1, LIST_GIVEN = 2 };
 int prepare(gapgpu_context& c, int nstruct, const int* n_atoms, const double* lattices, const int* pbcs, const int* d_mask,
-            double cutoff, bool rebuild, int precision);
+            double cutoff, int list_mode, int precision);
 int run_evaluation(gapgpu_context& c, int precision, const int* d_mask);
 int check_device_flags(gapgpu_context& c);
 // soap.cu

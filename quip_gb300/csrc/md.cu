@@ -63,7 +63,7 @@ int connect(gapgpu_md& md, bool force_rebuild) {
         rebuild = disp >= 0.5 * md.skin;
     }
     if ((rc = prepare(c, md.nstruct, md.n_atoms.data(), md.lattices.data(), md.pbcs.data(), nullptr,
-                      c.model->cutoff + md.skin, rebuild, c.precision)))
+                      c.model->cutoff + md.skin, rebuild ? LIST_BUILD : LIST_REFRESH, c.precision)))
         return rc;
     if (rebuild) {
         GG_CUDA(cudaMemcpyAsync(md.ref.p, c.pos.p, sizeof(double) * 3 * md.n, cudaMemcpyDeviceToDevice, c.stream));

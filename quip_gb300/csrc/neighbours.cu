@@ -300,6 +300,11 @@ __global__ void k_distances(long long P, const double* __restrict__ pos, const f
     if (r < 1e-10) atomicOr(bad, 2);
 }
 
+__global__ void k_zero_shift(long long P, int* __restrict__ ns) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p < P) ns[p] = pack_shift(0, 0, 0);
+}
+
 // Largest displacement since the list was built, minimum image on periodic axes
 // (distance_min_image of Connection.f95:1108).  Non-negative doubles order like their
 // bit patterns, so the maximum is an integer atomicMax.
@@ -633,6 +638,58 @@ int refresh_distances(gapgpu_context& c, const double* d_pos) {
         c.launches++;
     }
     GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
+int load_external_neighbours(gapgpu_context& c, int n, const std::vector<int>& off, const std::vector<int>& nj,
+                             const double* lattice, bool mixed) {
+    cudaStream_t st = c.stream;
+    const long long P = nj.size();
+    int rc;
+    const int pbc[3] = {0, 0, 0};
+    c.h_geoms.assign(1, GeomDev{});
+    GeomDev& g = c.h_geoms[0];
+    if ((rc = geom_begin(lattice, pbc, 0.0, g))) return rc;
+    g.atom_begin = 0;
+    g.atom_end = n;
+    for (int k = 0; k < 9; ++k) {
+        g.lat32[k] = (float)lattice[k];
+        g.lat_lo[k] = (float)(lattice[k] - (double)g.lat32[k]);
+    }
+    const size_t PP = std::max<long long>(P, 1);
+    if ((rc = c.geoms.ensure(sizeof(GeomDev))) || (rc = c.nbr_off.ensure(sizeof(int) * (n + 1))) ||
+        (rc = c.nbr_j.ensure(sizeof(int) * PP)) || (rc = c.nbr_d.ensure(sizeof(double4) * PP)) ||
+        (rc = c.nbr_s.ensure(sizeof(int) * PP)) || (rc = c.nbr_rev.ensure(sizeof(int) * PP)) ||
+        (rc = c.nbr_i.ensure(sizeof(int) * PP)) || (rc = c.total.ensure(sizeof(int) * 4)) ||
+        (rc = c.phi.ensure(sizeof(float4) * std::max(n, 1))) || (rc = c.plo.ensure(sizeof(float4) * std::max(n, 1))))
+        return rc;
+    std::vector<int> ni(P);
+    for (int a = 0; a < n; ++a)
+        for (int p = off[a]; p < off[a + 1]; ++p) ni[p] = a;
+    GG_CUDA(cudaMemcpyAsync(c.geoms.p, &g, sizeof(GeomDev), cudaMemcpyHostToDevice, st));
+    GG_CUDA(cudaMemcpyAsync(c.nbr_off.p, off.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st));
+    GG_CUDA(cudaMemsetAsync(c.total.p, 0, sizeof(int) * 4, st));
+    if (P > 0) {
+        GG_CUDA(cudaMemcpyAsync(c.nbr_j.p, nj.data(), sizeof(int) * P, cudaMemcpyHostToDevice, st));
+        GG_CUDA(cudaMemcpyAsync(c.nbr_i.p, ni.data(), sizeof(int) * P, cudaMemcpyHostToDevice, st));
+    }
+    c.n_pairs = P;
+    c.n_atoms_built = n;
+    c.nbr_mixed = mixed;
+    if (P > 0) {
+        int* bad = c.total.as<int>() + 2;
+        const unsigned nb = (unsigned)((P + 255) / 256);
+        k_zero_shift<<<nb, 256, 0, st>>>(P, c.nbr_s.as<int>());
+        if ((rc = refresh_distances(c, c.pos.as<double>()))) return rc;
+        k_reverse<<<nb, 256, 0, st>>>(P, c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_i.as<int>(), c.nbr_s.as<int>(),
+                                       c.nbr_rev.as<int>(), bad);
+        c.launches += 2;
+    }
+    int flags[4] = {0, 0, 0, 0};
+    GG_CUDA(cudaMemcpyAsync(flags, c.total.p, sizeof flags, cudaMemcpyDeviceToHost, st));
+    GG_CUDA(cudaStreamSynchronize(st));
+    if (flags[2] & 2) GG_FAIL(GAPGPU_ERR_ATOMS, "quip_lammps_wrapper: two atoms of a neighbour pair overlap exactly");
+    if (flags[2] & 4) GG_FAIL(GAPGPU_ERR_ARG, "neighbour list is not symmetric: give each local atom its full list");
     return GAPGPU_OK;
 }
 
