@@ -109,12 +109,24 @@ __global__ void k_wait_probe(long long limit, int* err) {
     atomicOr(err, 8);
 }
 
-__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* tm, int c0, int c1, uint64_t* bar) {
+// 2-D tiled TMA load with an L2 cache policy (createpolicy): the operand every CTA
+// re-reads (the sparse points) is kept in L2, the streamed one is evicted first.
+__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* tm, int c0, int c1, uint64_t* bar, uint64_t policy) {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            su32(dst)),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(su32(bar))
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, %3}], "
+        "[%4], %5;" ::"r"(su32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(su32(bar)), "l"(policy)
         : "memory");
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
 }
 
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
@@ -213,20 +225,20 @@ __device__ __forceinline__ void epilogue_chunk(const EpiParams& ep, int row, int
             uint4* ol = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(ep.out_lo) + (size_t)row * ep.ldo + col0);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                oh[q] = reinterpret_cast<const uint4*>(hi)[q];
-                ol[q] = reinterpret_cast<const uint4*>(lo)[q];
+                __stcs(oh + q, reinterpret_cast<const uint4*>(hi)[q]);
+                __stcs(ol + q, reinterpret_cast<const uint4*>(lo)[q]);
             }
         } else {
             float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
 #pragma unroll
             for (int q = 0; q < 8; ++q)
-                o[q] = make_float4(round_tf32(w[4 * q]), round_tf32(w[4 * q + 1]), round_tf32(w[4 * q + 2]),
-                                   round_tf32(w[4 * q + 3]));
+                __stcs(o + q, make_float4(round_tf32(w[4 * q]), round_tf32(w[4 * q + 1]), round_tf32(w[4 * q + 2]),
+                                          round_tf32(w[4 * q + 3])));
         }
     } else {
         float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        for (int q = 0; q < 8; ++q) __stcs(o + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
     }
 }
 
@@ -264,6 +276,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     if (warp == 0 && lane == 0) {
         // ---------------- TMA producer
+        const uint64_t pol_a = policy_evict_first(), pol_b = policy_evict_last();
         int it = 0;
         bool ok = true;
         for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
@@ -274,11 +287,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                 unsigned char* st = smem + (size_t)s * C::STAGE;
                 mbar_expect_tx(&full[s], C::STAGE);
                 const int kx = kc * C::KB;
-                tma_load(st, &tA0, kx, m0, &full[s]);
-                if constexpr (MODE == MODE_BF16X3) tma_load(st + C::TILE_A, &tA1, kx, m0, &full[s]);
+                tma_load(st, &tA0, kx, m0, &full[s], pol_a);
+                if constexpr (MODE == MODE_BF16X3) tma_load(st + C::TILE_A, &tA1, kx, m0, &full[s], pol_a);
                 unsigned char* sb = st + C::NOPS * C::TILE_A;
-                tma_load(sb, &tB0, kx, n0, &full[s]);
-                if constexpr (MODE == MODE_BF16X3) tma_load(sb + C::TILE_B, &tB1, kx, n0, &full[s]);
+                tma_load(sb, &tB0, kx, n0, &full[s], pol_b);
+                if constexpr (MODE == MODE_BF16X3) tma_load(sb + C::TILE_B, &tB1, kx, n0, &full[s], pol_b);
             }
         }
         if (!ok) {  // let the loads already issued land before the CTA exits
