@@ -32,16 +32,22 @@ namespace {
 
 // Constant block of one SOAP coordinate in the working precision R, uploaded once per
 // model and copied into shared memory by every block (offsets in elements of R):
-//   T[a][n] orthonormalising transform, rb[a] radial grid, cr[n] central-atom l = 0
+//   T[a][n] orthonormalising transform (also as Tt[n][a] and Tp[a][n], zero-padded to
+//   multiples of 4 for vector loads), rb[a] radial grid, cr[n] central-atom l = 0
 //   term, lf[l] = 1/sqrt(2l+1), yn[l*l+m] Ylm normalisation (sqrt2 folded in for m > 0),
 //   ra/rbb[l*l+m] Legendre recurrence P_lm = ra t P_(l-1)m - rbb P_(l-2)m (l >= m+2).
 struct SoapTab {
-    int T, rb, cr, lf, yn, ra, rbb, size;
+    int T, Tt, Tp, rb, cr, lf, yn, ra, rbb, size;
 };
+__host__ __device__ __forceinline__ int nmp_of(int nm) { return (nm + 3) & ~3; }
 __host__ __device__ __forceinline__ SoapTab soap_tab(int nm, int L) {
     SoapTab t;
     int o = 0;
+    const int NMP = nmp_of(nm);
     t.T = o; o += nm * nm;
+    o = (o + 3) & ~3;
+    t.Tt = o; o += nm * NMP;   // Tt[n][a] = T[a][n], rows zero-padded to NMP
+    t.Tp = o; o += NMP * NMP;  // Tp[a][n] = T[a][n], zero-padded to NMP x NMP
     t.rb = o; o += nm;
     t.cr = o; o += nm;
     t.lf = o; o += L;
@@ -224,8 +230,6 @@ constexpr int FWD_THREADS = 256;
 constexpr int TC = 32;   // neighbours staged per chunk in the forward kernel
 constexpr int TCB = 16;  // ... and in the backward kernel (dual Ylm staging is 4x larger)
 
-__host__ __device__ __forceinline__ int nmp_of(int nm) { return (nm + 3) & ~3; }
-
 // Per-chunk set-up by warp 0: species channel of each staged neighbour and, per
 // species, the list of staged neighbours in staging order (deterministic).
 template <int TCX>
@@ -363,10 +367,11 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     int* lst = spc + TC;                              // NS * TC
     int* lcnt = lst + NS * TC;                        // NS
     unsigned char* lofm = reinterpret_cast<unsigned char*>(lcnt + NS);  // L2
+    unsigned short* ptab = reinterpret_cast<unsigned short*>(lofm + ((L2 + 1) & ~1));  // n_pairs: ia << 8 | jb
     const int tid = threadIdx.x, bd = blockDim.x;
     load_tab(tab, K, tb.size);
     for (int k = tid; k < L2; k += bd) lofm[k] = (unsigned char)l_of_lm(k);
-    const int NA4 = NMP / 4, items = NS * L2 * NA4;
+    const int NA4 = NMP / 4, items = NS * L2 * NA4;  // NA4 also sizes the transform's vector loads
 
     R acc[FQ][4];
     int own_s[FQ], own_lm[FQ], own_a4[FQ];
@@ -448,13 +453,19 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
         const R* v = ct + (s * L2 + lm) * NMP;
         R va[MAX_NMAX];
 #pragma unroll
-        for (int a = 0; a < MAX_NMAX; ++a) va[a] = a < nm ? v[a] : (R)0;
+        for (int a4 = 0; a4 < MAX_NMAX / 4; ++a4)
+            if (a4 < NA4) load4(v + 4 * a4, va[4 * a4], va[4 * a4 + 1], va[4 * a4 + 2], va[4 * a4 + 3]);
         const bool centre = lm == 0 && (sc.centre_all || sc.species_Z[s] == zc || sc.species_Z[s] == 0);
         for (int n = 0; n < nm; ++n) {
+            const R* tr = K + tb.Tt + n * NMP;
             R x = 0;
 #pragma unroll
-            for (int a = 0; a < MAX_NMAX; ++a)
-                if (a < nm) x += K[tb.T + a * nm + n] * va[a];
+            for (int a4 = 0; a4 < MAX_NMAX / 4; ++a4)
+                if (a4 < NA4) {
+                    R t0, t1, t2, t3;
+                    load4(tr + 4 * a4, t0, t1, t2, t3);
+                    x += t0 * va[4 * a4] + t1 * va[4 * a4 + 1] + t2 * va[4 * a4 + 2] + t3 * va[4 * a4 + 3];
+                }
             if (centre) x += K[tb.cr + n];
             cs[(s * nm + n) * L2 + lm] = x;
         }
@@ -462,19 +473,29 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     __syncthreads();
     R* cg = c_out + (size_t)ci * sc.ncomp;
     for (int k = tid; k < sc.ncomp; k += bd) cg[k] = cs[k];
-    // power spectrum: one item per (ia, jb) pair, all l
+    // power spectrum: one item per (l, pair); pairs decoded once into a table
     R* ps = Ysm;
     R ssr = 0;
     for (int pr = tid; pr < sc.n_pairs; pr += bd) {
         int ia, jb;
         decode_pair(pr, ia, jb);
-        const R* ca = cs + ia * L2;
-        const R* cb = cs + jb * L2;
-        const R off2 = ia != jb ? (R)1.41421356237309504880 : (R)1;
-        for (int l = 0; l < L; ++l) {
-            R v = 0;
-            for (int m = l * l; m < (l + 1) * (l + 1); ++m) v += ca[m] * cb[m];
-            v *= off2 * K[tb.lf + l];
+        ptab[pr] = (unsigned short)(ia << 8 | jb);
+    }
+    __syncthreads();
+    if (tid < sc.n_pairs * L) {
+        Walk2 w(tid, bd, sc.n_pairs);
+        for (; w.i < L; w.next()) {
+            const int l = w.i, pr = w.j, ia = ptab[pr] >> 8, jb = ptab[pr] & 255;
+            const R* ca = cs + ia * L2 + l * l;
+            const R* cb = cs + jb * L2 + l * l;
+            R v0 = 0, v1 = 0;
+            int m = 0;
+            for (; m + 1 < 2 * l + 1; m += 2) {
+                v0 += ca[m] * cb[m];
+                v1 += ca[m + 1] * cb[m + 1];
+            }
+            if (m < 2 * l + 1) v0 += ca[m] * cb[m];
+            const R v = (v0 + v1) * (ia != jb ? (R)1.41421356237309504880 : (R)1) * K[tb.lf + l];
             ps[pr * L + l] = v;
             ssr += v * v;
         }
@@ -607,19 +628,23 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
     }
     __syncthreads();
     // h[s][lm][a] = sum_n T_an dE/dc[s][n][lm]: one thread per (s, lm)
+    const int NN4 = NMP / 4;
     for (int k = tid; k < NS * L2; k += bd) {
         const int s = k / L2, lm = k - s * L2;
         R vn[MAX_NMAX];
 #pragma unroll
         for (int n = 0; n < MAX_NMAX; ++n) vn[n] = n < nm ? dc[(s * nm + n) * L2 + lm] : (R)0;
         R* o = hs + (s * L2 + lm) * NMP;
-        for (int a = 0; a < NMP; ++a) {
+        for (int a = 0; a < NMP; ++a) {  // Tp rows beyond n_max are zero
+            const R* tr = K + tb.Tp + a * NMP;
             R x = 0;
-            if (a < nm) {
 #pragma unroll
-                for (int n = 0; n < MAX_NMAX; ++n)
-                    if (n < nm) x += K[tb.T + a * nm + n] * vn[n];
-            }
+            for (int n4 = 0; n4 < MAX_NMAX / 4; ++n4)
+                if (n4 < NN4) {
+                    R t0, t1, t2, t3;
+                    load4(tr + 4 * n4, t0, t1, t2, t3);
+                    x += t0 * vn[4 * n4] + t1 * vn[4 * n4 + 1] + t2 * vn[4 * n4 + 2] + t3 * vn[4 * n4 + 3];
+                }
             o[a] = x;
         }
     }
@@ -708,7 +733,7 @@ template <class R>
 size_t fwd_smem(const SoapConst& sc) {
     const int L = sc.l_max + 1, L2 = L * L, NS = sc.n_species;
     return sizeof(R) * ((size_t)soap_tab(sc.n_max, L).size + (size_t)((NS * sc.n_max * L2 + 3) & ~3) + fwd_region(sc)) +
-           sizeof(int) * (TC + NS * TC + NS) + (size_t)L2 + 64;
+           sizeof(int) * (TC + NS * TC + NS) + (size_t)L2 + 2 + 2 * (size_t)sc.n_pairs + 64;
 }
 template <class R>
 size_t bwd_smem(const SoapConst& sc) {
@@ -763,7 +788,13 @@ int upload_soap_tables(Coordinate& co) {
     const int nm = sp.n_max, L = sp.l_max + 1;
     const SoapTab tb = soap_tab(nm, L);
     std::vector<double> h(tb.size, 0.0);
+    const int NMP = nmp_of(nm);
     for (int k = 0; k < nm * nm; ++k) h[tb.T + k] = sp.T[k];
+    for (int a = 0; a < nm; ++a)
+        for (int n = 0; n < nm; ++n) {
+            h[tb.Tt + n * NMP + a] = sp.T[a * nm + n];
+            h[tb.Tp + a * NMP + n] = sp.T[a * nm + n];
+        }
     for (int a = 0; a < nm; ++a) { h[tb.rb + a] = sp.rb[a]; h[tb.cr + a] = sp.centre_R[a]; }
     for (int l = 0; l < L; ++l) {
         h[tb.lf + l] = 1.0 / std::sqrt((double)(2 * l + 1));

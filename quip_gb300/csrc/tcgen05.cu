@@ -194,7 +194,7 @@ struct EpiParams {
     int izeta;
     void* out_hi;         // W (bf16 hi or tf32 fp32) / G (fp32)
     void* out_lo;         // W lo (bf16x3)
-    double* epart;        // [rows x ntiles]
+    double* epart;        // [rows x ntiles]: energies per 64-column block
     int ntiles;
 };
 
@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         int t = 0;
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
             const int buf = t & 1;
-            const int m0 = (tile / n_tiles) * BM, n_blk = tile % n_tiles, n0 = n_blk * BN;
+            const int m0 = (tile / n_tiles) * BM, n0 = (tile % n_tiles) * BN;
             if (!mbar_wait(&tfull[buf], (t >> 1) & 1, &abort_flag, err, 4)) break;
             fence_after();
             const int row = m0 + q * 32 + lane;
@@ -349,9 +349,14 @@ __global__ void __launch_bounds__(THREADS, 1)
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_STRIDE + cc * 32, v);
                 if (row < ep.rows) epilogue_chunk<MODE, EPI>(ep, row, n0 + cc * 32, v, e_acc);
-            }
-            if constexpr (EPI == EPI_KERNEL) {
-                if (row < ep.rows) ep.epart[(size_t)row * ep.ntiles + n_blk] = (double)e_acc;
+                if constexpr (EPI == EPI_KERNEL) {
+                    // energies per 64-column block, whatever the tile width: the sum does not
+                    // depend on the autotuner's choice
+                    if (cc & 1) {
+                        if (row < ep.rows) ep.epart[(size_t)row * ep.ntiles + (n0 + cc * 32) / 64] = (double)e_acc;
+                        e_acc = 0.f;
+                    }
+                }
             }
             fence_before();
             __syncwarp();
@@ -497,7 +502,7 @@ int launch_bn(gapgpu_context& c, const CUtensorMap& a0, const CUtensorMap& a1, c
     const int smem = Cf::STAGES * Cf::STAGE + 1024;
     GG_CUDA(cudaFuncSetAttribute(k_tc_gemm<MODE, EPI, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     const int m_tiles = (rows + BM - 1) / BM, n_tiles = N / BN;
-    if (EPI == EPI_KERNEL) ep.ntiles = n_tiles;
+    if (EPI == EPI_KERNEL) ep.ntiles = N / 64;  // energy blocks of 64 columns
     const int ntiles = m_tiles * n_tiles;
     const int grid = std::min(ntiles, num_sms());
     k_tc_gemm<MODE, EPI, BN><<<grid, THREADS, smem, c.stream>>>(a0, a1, b0, b1, m_tiles, n_tiles, kchunks, ep, err);
@@ -573,7 +578,7 @@ int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows
     if (!BN) BN = pick_bn(MODE, N);
     CUtensorMap a0, a1, b0, b1;
     if ((rc = maps(BN, a0, a1, b0, b1))) return rc;
-    if (ntiles_out) *ntiles_out = N / BN;
+    if (ntiles_out) *ntiles_out = N / 64;
     return launch_any<MODE, EPI>(c, BN, a0, a1, b0, b1, rows, N, kchunks, ep, err);
 }
 
@@ -583,7 +588,7 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
     const size_t nq = (size_t)nc * Dp, nw = (size_t)nc * Mp;
     int rc;
     const size_t es = MODE == MODE_BF16X3 ? 2 : 4;
-    const int ntiles_max = Mp / 128;
+    const int ntiles_max = Mp / 64;
     if ((rc = c.Kbuf.ensure(es * nq)) || (rc = c.qlo.ensure(es * nq)) || (rc = c.Wbuf.ensure(es * nw)) ||
         (rc = c.Wlo.ensure(es * nw)) || (rc = c.epart.ensure(sizeof(double) * (size_t)nc * ntiles_max)) ||
         (rc = c.Gbuf.ensure(sizeof(float) * nq)) || (rc = c.total.ensure(sizeof(int) * 4)))
