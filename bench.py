@@ -384,17 +384,34 @@ def main():
         bound, pnote = "fp64", "cuBLAS DGEMM 4096^3 measured in this run"
         del a, b
         mult = 1.0
+    elif args.precision == "tf32":
+        # the TF32 tensor rate is not in MEASURED_PEAKS.json: measure cuBLAS TF32 here
+        torch.backends.cuda.matmul.allow_tf32 = True
+        a = torch.randn(8192, 8192, device="cuda")
+        b = torch.randn(8192, 8192, device="cuda")
+        for _ in range(3):
+            a @ b
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        peak = 10 * 2 * 8192 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
+        del a, b
+        bound, pnote = "tensor", "of measured: cuBLAS TF32 8192^3 in this run (bf16 burst %.1f TF/s in MEASURED_PEAKS.json)" % (
+            pk["bf16_tflops"])
+        mult = 1.0
     else:
-        mult = 3.0 if args.precision == "bf16x3" else 2.0
+        mult = 3.0
         peak = pk["bf16_tflops"] / mult
-        bound, pnote = "tensor", "of measured: bf16 burst %.1f TF/s / %g (%s)" % (
-            pk["bf16_tflops"], mult, "3 split-BF16 products" if mult == 3 else "TF32 at half the BF16 rate")
+        bound, pnote = "tensor", "of measured: bf16 burst %.1f TF/s / 3 (3 split-BF16 products)" % pk["bf16_tflops"]
     roofline = {"bound": bound, "kernel": "sparse-GP kernel GEMMs (k_tc_gemm x2: K = Q X^T with fused kernel epilogue, "
                                           "G = W X)",
                 "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s",
                 "frac": (gemm_tflops / peak) if gemm_tflops else None, "traffic": None, "peak_source": pnote,
                 "gemm_flops_per_atom": gemm_atom, "gemm_ms_per_step": gemm_ms,
-                "tensor_pipe_flops_per_atom": gemm_atom * mult}
+                "tensor_pipe_flops_per_atom": gemm_atom * (3.0 if args.precision == "bf16x3" else 1.0)}
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
