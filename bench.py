@@ -151,6 +151,19 @@ def cpu_reference(w, at, model_path, steps, warmup, sample_atoms=None):
             "seconds_per_sample": t}
 
 
+def max_over_ranks(t_local):
+    """The job's time under torchrun: the slowest rank's (replicas run independently;
+    this is the only collective, outside the timed region)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(t_local)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(t_local)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measure_batch(path, precision, structs, fp64_sample=48):
     """One batched evaluation of all structures (host arrays in and out, wall clock):
     first call, then repeated calls with CUDA-graph replay; the per-structure FP64 loop
@@ -217,7 +230,7 @@ def measure_serving(path, precision, pool, loads, seconds, replicas=64, seed=11)
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=150)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="sic32768", choices=sorted(WORKLOADS))
@@ -313,11 +326,7 @@ def main():
         t_wall0 = time.perf_counter()
         run = device_run(pot, args.steps, warmup)
         t_wall = time.perf_counter() - t_wall0
-    t_dev = run["t"]
-    if world > 1:
-        t = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = max_over_ranks(run["t"])
     value = world * n * args.steps / t_dev
     stage = run["stage"]
 
@@ -406,10 +415,20 @@ def main():
         mult = 3.0
         peak = pk["bf16_tflops"] / mult
         bound, pnote = "tensor", "of measured: bf16 burst %.1f TF/s / 3 (3 split-BF16 products)" % pk["bf16_tflops"]
-    roofline = {"bound": bound, "kernel": "sparse-GP kernel GEMMs (k_tc_gemm x2: K = Q X^T with fused kernel epilogue, "
-                                          "G = W X)",
+    # DRAM bytes of the two GEMM launches from the committed ncu capture of the 8192-atom
+    # case with this model (profiles/ncu_full_sic8192_tf32.md: 746+248 and 623+56 MB),
+    # scaled by the row count: the operand re-reads and the W/G writes grow with the rows
+    traffic = None
+    if args.precision == "tf32" and w["kind"] == "sic":
+        traffic = (746 + 248 + 623 + 56) * 1e6 * n / 8192
+    kernel = ("sparse-GP kernel GEMMs (FP64 SIMT k_gemm_nt_epi: K = Q X^T with fused kernel epilogue, k_gemm_nn: "
+              "G = W X)" if args.precision == "fp64" else
+              "sparse-GP kernel GEMMs (k_tc_gemm x2: K = Q X^T with fused kernel epilogue, G = W X)")
+    roofline = {"bound": bound, "kernel": kernel,
                 "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s",
-                "frac": (gemm_tflops / peak) if gemm_tflops else None, "traffic": None, "peak_source": pnote,
+                "frac": (gemm_tflops / peak) if gemm_tflops else None, "traffic": traffic,
+                "traffic_note": "DRAM bytes per step of the two GEMM launches, ncu capture at 8192 atoms scaled by the "
+                                "row count" if traffic else None, "peak_source": pnote,
                 "gemm_flops_per_atom": gemm_atom, "gemm_ms_per_step": gemm_ms,
                 "tensor_pipe_flops_per_atom": gemm_atom * (3.0 if args.precision == "bf16x3" else 1.0)}
 

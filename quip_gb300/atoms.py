@@ -113,3 +113,43 @@ def read_xyz(path, index=None):
     if index is not None:
         return frames[index]
     return frames
+
+
+def _fmt_value(v):
+    if isinstance(v, (bool, np.bool_)):
+        return "T" if v else "F"
+    if isinstance(v, (int, np.integer)):
+        return "%d" % v
+    if isinstance(v, (float, np.floating)):
+        return "%.17g" % v
+    v = str(v)
+    return '"%s"' % v if (" " in v or "=" in v) else v
+
+
+def write_xyz(path, frames, properties=("force",), mode="w"):
+    """Write frames as extended XYZ in the header conventions read_xyz (and the
+    reference's reader, src/libAtoms/xyz.c) accept: Lattice="..." (cell vectors in
+    order), Properties=species:S:1:pos:R:3[:name:R:k...], pbc="T T T", info entries as
+    key=value.  Per-atom arrays named in `properties` are written when present (N or
+    N x k floats).  Positions and floats keep 17 significant digits, so a write/read
+    round trip is exact."""
+    if isinstance(frames, Atoms):
+        frames = [frames]
+    with open(path, mode) as f:
+        for at in frames:
+            extra = []
+            for name in properties:
+                if name in at.arrays:
+                    a = np.asarray(at.arrays[name], dtype=np.float64)
+                    extra.append((name, a.reshape(len(at), -1)))
+            props = "species:S:1:pos:R:3" + "".join(":%s:R:%d" % (nm, a.shape[1]) for nm, a in extra)
+            hdr = ['Lattice="%s"' % " ".join("%.17g" % x for x in at.lattice.T.ravel()),
+                   "Properties=%s" % props, 'pbc="%s"' % " ".join("T" if p else "F" for p in at.pbc)]
+            hdr += ["%s=%s" % (k, _fmt_value(v)) for k, v in at.info.items()]
+            f.write("%d\n%s\n" % (len(at), " ".join(hdr)))
+            for i in range(len(at)):
+                cols = [SYMBOLS[int(at.numbers[i])]] + ["%.17g" % x for x in at.positions[i]]
+                for _, a in extra:
+                    cols += ["%.17g" % x for x in a[i]]
+                f.write(" ".join(cols) + "\n")
+

@@ -126,3 +126,23 @@ def test_descriptor_string_parsing():
     assert models.descriptor_dim(d) == 1891
     assert models.descriptor_dim(models.soap_descriptor_string(5.0, 8, 6)) == 253
     assert models.descriptor_dim("distance_2b cutoff=4 Z1=1 Z2=8") == 1
+
+
+def test_extxyz_write_read_round_trip(tmp_path, golden):
+    from quip_gb300.atoms import read_xyz, write_xyz
+    frames = read_xyz(os.path.join(golden, "Si.np1.xyz"))[:4]
+    t = models.random_triclinic(20, rng=np.random.default_rng(3))
+    t.arrays["force"] = np.random.default_rng(4).normal(size=(20, 3))
+    t.info["energy"] = -12.5
+    p = str(tmp_path / "out.xyz")
+    write_xyz(p, frames + [t])
+    back = read_xyz(p)
+    assert len(back) == 5
+    for a, b in zip(frames + [t], back):
+        np.testing.assert_array_equal(a.numbers, b.numbers)
+        np.testing.assert_array_equal(a.positions, b.positions)
+        np.testing.assert_array_equal(a.lattice, b.lattice)
+        np.testing.assert_array_equal(a.pbc, b.pbc)
+    np.testing.assert_array_equal(back[-1].arrays["force"], t.arrays["force"])
+    assert back[-1].info["energy"] == -12.5
+
