@@ -59,20 +59,9 @@ __host__ __device__ __forceinline__ SoapTab soap_tab(int nm, int L) {
 }
 
 template <class R>
-struct alignas(4 * sizeof(R)) Dual {  // value and gradient with respect to the neighbour's displacement
+struct alignas(4 * sizeof(R)) Dual {  // a value and three derivatives
     R v, x, y, z;
 };
-template <class R> __device__ __forceinline__ Dual<R> dmul(const Dual<R>& a, const Dual<R>& b) {
-    return {a.v * b.v, a.x * b.v + a.v * b.x, a.y * b.v + a.v * b.y, a.z * b.v + a.v * b.z};
-}
-template <class R> __device__ __forceinline__ Dual<R> dsub(const Dual<R>& a, const Dual<R>& b) {
-    return {a.v - b.v, a.x - b.x, a.y - b.y, a.z - b.z};
-}
-template <class R> __device__ __forceinline__ Dual<R> dadd(const Dual<R>& a, const Dual<R>& b) {
-    return {a.v + b.v, a.x + b.x, a.y + b.y, a.z + b.z};
-}
-template <class R> __device__ __forceinline__ Dual<R> dscale(R s, const Dual<R>& a) { return {s * a.v, s * a.x, s * a.y, s * a.z}; }
-
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
 __device__ __forceinline__ float rexp(float x) { return __expf(x); }
 __device__ __forceinline__ double rcos(double x) { return cos(x); }
@@ -126,36 +115,51 @@ __device__ void ylm_column(int m, int L, R xr, R yr, R t, const R* __restrict__ 
     }
 }
 
-// Same column with gradients (dual arithmetic on the neighbour's x, y, z), from the
-// unit vector u and 1/r: d u_a / d x_b = (delta_ab - u_a u_b) / r.
+// Same column with the gradient of its Cartesian form N_lm Q_lm(u_z) Re/Im (u_x + i u_y)^m
+// with respect to the components of u taken as independent: d/du_x (u_x + i u_y)^m =
+// m (u_x + i u_y)^(m-1), d/du_y = i m (u_x + i u_y)^(m-1), and Q'_lm follows Q_lm's
+// recurrence.  Y[lm] = (Y, dY/du_x, dY/du_y, dY/du_z); the tangential projection
+// (I - u u^T) / r is applied once per neighbour after the contraction.
 template <class R>
-__device__ void ylm_column_grad(int m, int L, R xr, R yr, R zr, R ir, const R* __restrict__ K, const SoapTab& tb,
+__device__ void ylm_column_cart(int m, int L, R xr, R yr, R zr, const R* __restrict__ K, const SoapTab& tb,
                                 Dual<R>* Y) {
-    const Dual<R> X = {xr, (1 - xr * xr) * ir, -xr * yr * ir, -xr * zr * ir};
-    const Dual<R> Yv = {yr, -yr * xr * ir, (1 - yr * yr) * ir, -yr * zr * ir};
-    const Dual<R> T = {zr, -zr * xr * ir, -zr * yr * ir, (1 - zr * zr) * ir};
-    Dual<R> cm = {1, 0, 0, 0}, sm = {0, 0, 0, 0};
+    R cm = 1, sm = 0, cp = 1, sp = 0;  // (u_x + i u_y)^m and ^(m-1)
     for (int k = 0; k < m; ++k) {
-        Dual<R> c2 = dsub(dmul(cm, X), dmul(sm, Yv));
-        sm = dadd(dmul(sm, X), dmul(cm, Yv));
+        cp = cm;
+        sp = sm;
+        const R c2 = cm * xr - sm * yr;
+        sm = sm * xr + cm * yr;
         cm = c2;
     }
     R qmm = 1;
     for (int k = 1; k <= 2 * m - 1; k += 2) qmm *= (R)k;
-    Dual<R> q1 = {0, 0, 0, 0}, q2 = {0, 0, 0, 0};
+    R q1 = 0, q2 = 0, d1 = 0, d2 = 0;
+    const R fm = (R)m;
     for (int l = m; l < L; ++l) {
         const int i = l * l + m;
-        Dual<R> q;
-        if (l == m) q = {qmm, 0, 0, 0};
-        else if (l == m + 1) q = dscale((R)(2 * m + 1) * qmm, T);
-        else q = dsub(dscale(K[tb.ra + i], dmul(T, q1)), dscale(K[tb.rbb + i], q2));
+        R q, d;
+        if (l == m) {
+            q = qmm;
+            d = 0;
+        } else if (l == m + 1) {
+            q = (R)(2 * m + 1) * zr * qmm;
+            d = (R)(2 * m + 1) * qmm;
+        } else {
+            const R ra = K[tb.ra + i], rb = K[tb.rbb + i];
+            q = ra * zr * q1 - rb * q2;
+            d = ra * (q1 + zr * d1) - rb * d2;
+        }
         q2 = q1;
         q1 = q;
+        d2 = d1;
+        d1 = d;
         const R nrm = K[tb.yn + i];
-        if (m == 0) Y[l * l + l] = dscale(nrm, q);
+        const R nq = nrm * q, nd = nrm * d;
+        if (m == 0) Y[l * l + l] = {nq, (R)0, (R)0, nd};
         else {
-            Y[l * l + l + m] = dscale(nrm, dmul(q, cm));
-            Y[l * l + l - m] = dscale(nrm, dmul(q, sm));
+            const R a = nq * fm;
+            Y[l * l + l + m] = {nq * cm, a * cp, -a * sp, nd * cm};
+            Y[l * l + l - m] = {nq * sm, a * sp, a * cp, nd * sm};
         }
     }
 }
@@ -664,7 +668,7 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
             for (; w.i < cnt; w.next()) {
                 if (spc[w.i] < 0) continue;
                 const R* u = dsm + DS * w.i;
-                ylm_column_grad<R>(w.j, L, u[0], u[1], u[2], u[3], K, tb, Yd + w.i * L2);
+                ylm_column_cart<R>(w.j, L, u[0], u[1], u[2], K, tb, Yd + w.i * L2);
             }
         }
         if (tid < cnt * NMP) {
@@ -686,25 +690,33 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
             const int s = spc[t];
             if (s < 0) continue;  // warp-uniform
             const R* u = dsm + DS * t;
-            const R ux = u[0], uy = u[1], uz = u[2];
+            const R ux = u[0], uy = u[1], uz = u[2], ir = u[3];
             const R f = fcs[t], df = dfcs[t];
-            R fx = 0, fy = 0, fz = 0;
+            // radial part sum_lm (f w + f' u) Y and angular part sum_lm f u dY/du (unprojected)
+            R ar = 0, gx = 0, gy = 0, gz = 0;
             for (int lm = lane; lm < L2; lm += 32) {
                 const int l = lofm[lm];
                 R uu = 0, ww = 0;
                 dot2(hs + (s * L2 + lm) * NMP, Ism + (t * L + l) * NMP, dIsm + (t * L + l) * NMP, NMP, uu, ww);
                 const Dual<R> y = Yd[t * L2 + lm];
-                const R rad = (f * ww + df * uu) * y.v, ang = f * uu;
-                fx += rad * ux + ang * y.x;
-                fy += rad * uy + ang * y.y;
-                fz += rad * uz + ang * y.z;
+                const R ang = f * uu;
+                ar += (f * ww + df * uu) * y.v;
+                gx += ang * y.x;
+                gy += ang * y.y;
+                gz += ang * y.z;
             }
             for (int o = 16; o > 0; o >>= 1) {
-                fx += __shfl_xor_sync(0xffffffffu, fx, o);
-                fy += __shfl_xor_sync(0xffffffffu, fy, o);
-                fz += __shfl_xor_sync(0xffffffffu, fz, o);
+                ar += __shfl_xor_sync(0xffffffffu, ar, o);
+                gx += __shfl_xor_sync(0xffffffffu, gx, o);
+                gy += __shfl_xor_sync(0xffffffffu, gy, o);
+                gz += __shfl_xor_sync(0xffffffffu, gz, o);
             }
             if (lane == 0) {
+                // f = ar u + (I - u u^T) g / r
+                const R gu = gx * ux + gy * uy + gz * uz;
+                const R fx = ar * ux + (gx - gu * ux) * ir;
+                const R fy = ar * uy + (gy - gu * uy) * ir;
+                const R fz = ar * uz + (gz - gu * uz) * ir;
                 const size_t p = (size_t)(base + t);
                 fpair[3 * p] += (double)fx;
                 fpair[3 * p + 1] += (double)fy;
