@@ -47,7 +47,7 @@ struct gapgpu_context {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     // atoms
-    gapgpu::DBuf pos, Z, mask, out_e, out_f, out_v, out_le, out_lv;
+    gapgpu::DBuf pos, Z, mask, out_e, out_f, out_le, out_lv;
     // cells and neighbours
     gapgpu::DBuf cell_key, cell_key2, atom_idx, atom_idx2, cell_start, cell_end, ms, cub_tmp, minmax;
     gapgpu::DBuf nbr_cnt, nbr_off, nbr_j, nbr_d, nbr_s, nbr_rev, nbr_i, wpos, total, geoms, sid, dispmax, phi, plo;
@@ -57,7 +57,7 @@ struct gapgpu_context {
     // per pair / per atom accumulators
     gapgpu::DBuf fpair, epair, eatom, redpart;
     // SOAP / GP workspace
-    gapgpu::DBuf flags, centres, ncent, coef, qbuf, qlo, pnorm, Kbuf, Wbuf, Wlo, epart, ecent, Gbuf, scratch;
+    gapgpu::DBuf flags, centres, ncent, qbuf, qlo, pnorm, Kbuf, Wbuf, Wlo, epart, ecent, Gbuf, scratch;
     int* cur_centres = nullptr;               // centre list of the coordinate being evaluated
     std::vector<int> nc_coord;                // centres per coordinate (prepare phase)
     gapgpu::DBuf chunks, schunk;              // segmented-reduction tables (per batch)
@@ -79,10 +79,10 @@ struct gapgpu_context {
     long long launches = 0;
     gapgpu::Timings t;
     std::vector<gapgpu::DBuf*> buffers() {
-        return {&pos, &Z, &mask, &out_e, &out_f, &out_v, &out_le, &out_lv, &cell_key, &cell_key2, &atom_idx, &atom_idx2,
+        return {&pos, &Z, &mask, &out_e, &out_f, &out_le, &out_lv, &cell_key, &cell_key2, &atom_idx, &atom_idx2,
                 &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev,
                 &nbr_i, &wpos, &total, &geoms, &sid, &dispmax, &phi, &plo, &fpair, &epair, &eatom, &redpart, &flags, &centres,
-                &ncent, &coef, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf, &Wlo, &epart, &ecent, &Gbuf, &scratch, &chunks, &schunk};
+                &ncent, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf, &Wlo, &epart, &ecent, &Gbuf, &scratch, &chunks, &schunk};
     }
     std::vector<const gapgpu::DBuf*> buffers() const {
         std::vector<gapgpu::DBuf*> b = const_cast<gapgpu_context*>(this)->buffers();

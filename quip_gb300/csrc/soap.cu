@@ -293,6 +293,12 @@ __device__ __forceinline__ void dot2(const double* __restrict__ h, const double*
 }
 
 template <class R>
+__device__ __forceinline__ R warp_sum(R v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <class R>
 __device__ __forceinline__ void load_tab(const R* __restrict__ tab, R* K, int n) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) K[k] = tab[k];
 }
@@ -504,17 +510,21 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
             ssr += v * v;
         }
     }
-    typedef cub::BlockReduce<double, FWD_THREADS> BR;
-    __shared__ typename BR::TempStorage tmps;
-    const double tot = BR(tmps).Sum((double)ssr);
-    __shared__ double s_inv;
+    // FP32 partial sums per warp, combined in FP64
+    __shared__ double s_wsum[FWD_THREADS / 32];
+    __shared__ R s_inv;
+    ssr = warp_sum(ssr);
+    if ((tid & 31) == 0) s_wsum[tid >> 5] = (double)ssr;
+    __syncthreads();
     if (tid == 0) {
+        double tot = 0;
+        for (int w = 0; w < FWD_THREADS / 32; ++w) tot += s_wsum[w];
         const double nrm = sqrt(tot);
         pnorm[ci] = nrm;
-        s_inv = sc.normalise ? 1.0 / nrm : 1.0;
+        s_inv = sc.normalise ? (R)(1.0 / nrm) : (R)1;
     }
     __syncthreads();
-    const R inv = (R)s_inv;
+    const R inv = s_inv;
     const int np = sc.n_pairs * L;
     R* qg = q_out + (size_t)ci * sc.dpad;
     for (int k = tid; k < sc.dpad; k += bd) {
@@ -593,16 +603,20 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
     const R* gg = G + (size_t)ci * sc.dpad;
     R part = 0;
     for (int k = tid; k < np; k += bd) part += qg[k] * gg[k];
-    typedef cub::BlockReduce<double, BWD_THREADS> BR;
-    __shared__ typename BR::TempStorage tmps;
-    const double tot = BR(tmps).Sum((double)part);
-    __shared__ double s_qg, s_inv;
+    __shared__ double s_wsum[BWD_WARPS];
+    __shared__ R s_sc[2];
+    __shared__ R s_f[3 * TCB];  // per-pair forces of the last chunk, flushed during the next staging
+    part = warp_sum(part);
+    if (lane == 0) s_wsum[wid] = (double)part;
+    __syncthreads();
     if (tid == 0) {
-        s_qg = tot;
-        s_inv = 1.0 / pnorm[ci];
+        double tot = 0;
+        for (int w = 0; w < BWD_WARPS; ++w) tot += s_wsum[w];
+        s_sc[0] = (R)tot;
+        s_sc[1] = (R)(1.0 / pnorm[ci]);
     }
     __syncthreads();
-    const R sq = (R)s_qg, inv = (R)s_inv;
+    const R sq = s_sc[0], inv = s_sc[1];
     for (int pr = tid; pr < sc.n_pairs; pr += bd) {
         int ia, jb;
         decode_pair(pr, ia, jb);
@@ -654,6 +668,7 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
     }
     const R alpha = (R)sc.alpha;
     const int p0 = off[atom], p1 = off[atom + 1];
+    int prev = p0, prev_cnt = 0;
     for (int base = p0; base < p1; base += TCB) {
         const int cnt = min(TCB, p1 - base);
         __syncthreads();
@@ -661,7 +676,11 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
         else if (tid - 32 < cnt) {
             const int t = tid - 32;
             stage_neighbour<R>(sc, nd[base + t], dsm + DS * t, fcs + t, dfcs + t);
+        } else if (tid >= 64 && tid - 64 < 3 * prev_cnt) {
+            fpair[3 * (size_t)prev + (tid - 64)] += (double)s_f[tid - 64];
         }
+        prev = base;
+        prev_cnt = cnt;
         __syncthreads();
         if (tid < cnt * L) {
             Walk2 w(tid, bd, L);
@@ -688,7 +707,10 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
         __syncthreads();
         for (int t = wid; t < cnt; t += BWD_WARPS) {
             const int s = spc[t];
-            if (s < 0) continue;  // warp-uniform
+            if (s < 0) {  // warp-uniform
+                if (lane < 3) s_f[3 * t + lane] = 0;
+                continue;
+            }
             const R* u = dsm + DS * t;
             const R ux = u[0], uy = u[1], uz = u[2], ir = u[3];
             const R f = fcs[t], df = dfcs[t];
@@ -717,13 +739,14 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
                 const R fx = ar * ux + (gx - gu * ux) * ir;
                 const R fy = ar * uy + (gy - gu * uy) * ir;
                 const R fz = ar * uz + (gz - gu * uz) * ir;
-                const size_t p = (size_t)(base + t);
-                fpair[3 * p] += (double)fx;
-                fpair[3 * p + 1] += (double)fy;
-                fpair[3 * p + 2] += (double)fz;
+                s_f[3 * t] = fx;
+                s_f[3 * t + 1] = fy;
+                s_f[3 * t + 2] = fz;
             }
         }
     }
+    __syncthreads();
+    if (tid < 3 * prev_cnt) fpair[3 * (size_t)prev + tid] += (double)s_f[tid];
 }
 
 __global__ void k_centre_flags(int n, const int* __restrict__ Z, const int* __restrict__ mask, SoapConst sc, int nZ,
