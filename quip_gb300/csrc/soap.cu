@@ -272,17 +272,26 @@ __device__ __forceinline__ void stage_neighbour(const SoapConst& sc, const doubl
 }
 constexpr int DS = 5;  // staged values per neighbour: ux, uy, uz, 1/r, r
 
-// sum_e h[e] * x[e] over NMP entries (NMP a multiple of 4), two right-hand sides.
+// sum_e h[e] * x[e] over NMP entries (NMP a multiple of 4), two right-hand sides.  The
+// FP32 form keeps even and odd entries in the two halves of packed FP32x2 FMAs.
 __device__ __forceinline__ void dot2(const float* __restrict__ h, const float* __restrict__ x, const float* __restrict__ y,
                                      int NMP, float& u, float& w) {
     const float4* h4 = reinterpret_cast<const float4*>(h);
     const float4* x4 = reinterpret_cast<const float4*>(x);
     const float4* y4 = reinterpret_cast<const float4*>(y);
-    for (int a = 0; a < NMP / 4; ++a) {
-        const float4 hh = h4[a], xx = x4[a], yy = y4[a];
-        u += hh.x * xx.x + hh.y * xx.y + hh.z * xx.z + hh.w * xx.w;
-        w += hh.x * yy.x + hh.y * yy.y + hh.z * yy.z + hh.w * yy.w;
-    }
+    float2 uu = make_float2(0.f, 0.f), ww = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < MAX_NMAX / 4; ++a)
+        if (a < NMP / 4) {
+            const float4 hh = h4[a], xx = x4[a], yy = y4[a];
+            const float2 h0 = make_float2(hh.x, hh.y), h1 = make_float2(hh.z, hh.w);
+            uu = __ffma2_rn(h0, make_float2(xx.x, xx.y), uu);
+            ww = __ffma2_rn(h0, make_float2(yy.x, yy.y), ww);
+            uu = __ffma2_rn(h1, make_float2(xx.z, xx.w), uu);
+            ww = __ffma2_rn(h1, make_float2(yy.z, yy.w), ww);
+        }
+    u += uu.x + uu.y;
+    w += ww.x + ww.y;
 }
 __device__ __forceinline__ void dot2(const double* __restrict__ h, const double* __restrict__ x,
                                      const double* __restrict__ y, int NMP, double& u, double& w) {
@@ -296,6 +305,28 @@ template <class R>
 __device__ __forceinline__ R warp_sum(R v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+// Sums of four values over the warp, returned in every lane: a transposing butterfly
+// (each of the first two exchanges sends half of the lane's partial sums), then the
+// four totals are gathered from lanes 0, 8, 16 and 24.
+template <class R>
+__device__ __forceinline__ void warp_sum4(R& a, R& b, R& c, R& d) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool h16 = lane & 16, h8 = lane & 8;
+    R k0 = h16 ? c : a, k1 = h16 ? d : b;
+    k0 += __shfl_xor_sync(full, h16 ? a : c, 16);
+    k1 += __shfl_xor_sync(full, h16 ? b : d, 16);
+    R k = h8 ? k1 : k0;
+    k += __shfl_xor_sync(full, h8 ? k0 : k1, 8);
+    k += __shfl_xor_sync(full, k, 4);
+    k += __shfl_xor_sync(full, k, 2);
+    k += __shfl_xor_sync(full, k, 1);
+    a = __shfl_sync(full, k, 0);
+    b = __shfl_sync(full, k, 8);
+    c = __shfl_sync(full, k, 16);
+    d = __shfl_sync(full, k, 24);
 }
 
 template <class R>
@@ -727,12 +758,7 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
                 gy += ang * y.y;
                 gz += ang * y.z;
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                ar += __shfl_xor_sync(0xffffffffu, ar, o);
-                gx += __shfl_xor_sync(0xffffffffu, gx, o);
-                gy += __shfl_xor_sync(0xffffffffu, gy, o);
-                gz += __shfl_xor_sync(0xffffffffu, gz, o);
-            }
+            warp_sum4(ar, gx, gy, gz);
             if (lane == 0) {
                 // f = ar u + (I - u u^T) g / r
                 const R gu = gx * ux + gy * uy + gz * uz;
