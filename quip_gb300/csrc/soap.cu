@@ -430,6 +430,11 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
         acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0;
     }
     const R alpha = (R)sc.alpha;
+    const int NPAD = NMP - nm;  // basis columns n_max..NMP-1 of the staged radial rows stay zero
+    for (int k = tid; k < TC * L * NPAD; k += bd) {
+        const int row = k / NPAD;
+        Ism[row * NMP + nm + (k - row * NPAD)] = 0;
+    }
     const int p0 = off[atom], p1 = off[atom + 1];
     for (int base = p0; base < p1; base += TC) {
         const int cnt = min(TC, p1 - base);
@@ -440,25 +445,21 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
             stage_neighbour<R>(sc, nd[base + t], dsm + DS * t, fcs + t, (R*)nullptr);
         }
         __syncthreads();
-        if (tid < cnt * L) {
-            Walk2 w(tid, bd, L);
-            for (; w.i < cnt; w.next()) {
-                if (spc[w.i] < 0) continue;
-                const R* u = dsm + DS * w.i;
-                ylm_column<R>(w.j, L, u[0], u[1], u[2], K, tb, Ysm + w.i * L2);
-            }
-        }
-        if (tid < cnt * NMP) {
-            Walk2 w(tid, bd, NMP);
-            for (; w.i < cnt; w.next()) {
-                const int t = w.i, a = w.j;
+        // Ylm columns and radial rows of the staged neighbours as one task list: first the
+        // columns, m descending with the neighbour fastest (a warp's lanes share m, so the
+        // recurrences run equally long), then the rows (t, a) of the n_max basis functions
+        const int nY = cnt * L, nT = nY + cnt * nm;
+        for (int k = tid; k < nT; k += bd) {
+            if (k < nY) {
+                const int mi = k / cnt, t = k - mi * cnt;
                 if (spc[t] < 0) continue;
-                R* out = Ism + t * L * NMP + a;
-                if (a >= nm) {
-                    for (int l = 0; l < L; ++l) out[l * NMP] = 0;
-                    continue;
-                }
-                radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, fcs[t], out, (R*)nullptr, NMP);
+                const R* u = dsm + DS * t;
+                ylm_column<R>(L - 1 - mi, L, u[0], u[1], u[2], K, tb, Ysm + t * L2);
+            } else {
+                const int k2 = k - nY, t = k2 / nm, a = k2 - t * nm;
+                if (spc[t] < 0) continue;
+                radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, fcs[t], Ism + t * L * NMP + a,
+                                      (R*)nullptr, NMP);
             }
         }
         __syncthreads();
@@ -710,29 +711,33 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
         } else if (tid >= 64 && tid - 64 < 3 * prev_cnt) {
             fpair[3 * (size_t)prev + (tid - 64)] += (double)s_f[tid - 64];
         }
+        if (base == p0 && tid >= 64) {
+            // basis columns n_max..NMP-1 of the staged radial rows stay zero (the staging
+            // area held the pre-phase buffers until now)
+            const int NPAD = NMP - nm;
+            for (int k = tid - 64; k < TCB * L * NPAD; k += bd - 64) {
+                const int row = k / NPAD, col = nm + (k - row * NPAD);
+                Ism[row * NMP + col] = 0;
+                dIsm[row * NMP + col] = 0;
+            }
+        }
         prev = base;
         prev_cnt = cnt;
         __syncthreads();
-        if (tid < cnt * L) {
-            Walk2 w(tid, bd, L);
-            for (; w.i < cnt; w.next()) {
-                if (spc[w.i] < 0) continue;
-                const R* u = dsm + DS * w.i;
-                ylm_column_cart<R>(w.j, L, u[0], u[1], u[2], K, tb, Yd + w.i * L2);
-            }
-        }
-        if (tid < cnt * NMP) {
-            Walk2 w(tid, bd, NMP);
-            for (; w.i < cnt; w.next()) {
-                const int t = w.i, a = w.j;
+        // one task list as in the forward kernel: Ylm columns (m descending, neighbour
+        // fastest), then the radial rows (t, a) with their r-derivatives
+        const int nY = cnt * L, nT = nY + cnt * nm;
+        for (int k = tid; k < nT; k += bd) {
+            if (k < nY) {
+                const int mi = k / cnt, t = k - mi * cnt;
                 if (spc[t] < 0) continue;
-                R* o = Ism + t * L * NMP + a;
-                R* od = dIsm + t * L * NMP + a;
-                if (a >= nm) {
-                    for (int l = 0; l < L; ++l) { o[l * NMP] = 0; od[l * NMP] = 0; }
-                    continue;
-                }
-                radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, (R)1, o, od, NMP);
+                const R* u = dsm + DS * t;
+                ylm_column_cart<R>(L - 1 - mi, L, u[0], u[1], u[2], K, tb, Yd + t * L2);
+            } else {
+                const int k2 = k - nY, t = k2 / nm, a = k2 - t * nm;
+                if (spc[t] < 0) continue;
+                radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, (R)1, Ism + t * L * NMP + a,
+                                      dIsm + t * L * NMP + a, NMP);
             }
         }
         __syncthreads();
