@@ -234,18 +234,37 @@ constexpr int FWD_THREADS = 256;
 constexpr int TC = 32;   // neighbours staged per chunk in the forward kernel
 constexpr int TCB = 16;  // ... and in the backward kernel (dual Ylm staging is 4x larger)
 
+// Neighbour data of one chunk, loaded into registers one chunk ahead of its staging so
+// that the dependent loads (list -> atomic number) overlap the previous chunk's work:
+// warp 0 holds |r| and Z of neighbour base + lane (species lists), the next threads
+// hold the displacement of neighbour base + (tid - 32) (staging).
+struct ChunkFetch {
+    double r = 0.0;
+    int z = 0;
+    double4 d = {0.0, 0.0, 0.0, 0.0};
+    template <int TCX>
+    __device__ __forceinline__ void load(int b, int p1, const int* __restrict__ Z, const int* __restrict__ nj,
+                                         const double4* __restrict__ nd) {
+        const int c = min(TCX, p1 - b), tid = threadIdx.x;
+        if (tid < 32) {
+            if (tid < c) {
+                r = nd[b + tid].w;
+                z = Z[nj[b + tid]];
+            }
+        } else if (tid - 32 < c) {
+            d = nd[b + tid - 32];
+        }
+    }
+};
+
 // Per-chunk set-up by warp 0: species channel of each staged neighbour and, per
 // species, the list of staged neighbours in staging order (deterministic).
 template <int TCX>
-__device__ __forceinline__ void build_species_lists(const SoapConst& sc, int base, int cnt, const int* __restrict__ Z,
-                                                    const int* __restrict__ nj, const double4* __restrict__ nd, int* spc,
+__device__ __forceinline__ void build_species_lists(const SoapConst& sc, int cnt, const ChunkFetch& f, int* spc,
                                                     int* lst, int* lcnt) {
     const int lane = threadIdx.x & 31;
     int s = -1;
-    if (lane < cnt) {
-        const double r = nd[base + lane].w;
-        s = (r < sc.rc) ? species_channel(sc, Z[nj[base + lane]]) : -1;
-    }
+    if (lane < cnt) s = (f.r < sc.rc) ? species_channel(sc, f.z) : -1;
     if (lane < TCX) spc[lane] = s;
     const unsigned lt = (1u << lane) - 1u;
     for (int k = 0; k < sc.n_species; ++k) {
@@ -301,6 +320,31 @@ __device__ __forceinline__ void dot2(const double* __restrict__ h, const double*
     }
 }
 
+// d0 = sum_b h[b * NNP] c[b * L2], d1 = sum_b h[b * NNP + 1] c[b * L2] (h 8-byte aligned)
+__device__ __forceinline__ void hrow2(const float* __restrict__ h, const float* __restrict__ c, int NN, int NNP, int L2,
+                                      float& d0, float& d1) {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int b = 0; b < NN; ++b) {
+        const float2 hv = *reinterpret_cast<const float2*>(h + b * NNP);
+        const float cv = c[b * L2];
+        acc = __ffma2_rn(hv, make_float2(cv, cv), acc);
+    }
+    d0 = acc.x;
+    d1 = acc.y;
+}
+__device__ __forceinline__ void hrow2(const double* __restrict__ h, const double* __restrict__ c, int NN, int NNP,
+                                      int L2, double& d0, double& d1) {
+    double x = 0, y = 0;
+    for (int b = 0; b < NN; ++b) {
+        const double cv = c[b * L2];
+        x += h[b * NNP] * cv;
+        y += h[b * NNP + 1] * cv;
+    }
+    d0 = x;
+    d1 = y;
+}
+
 template <class R>
 __device__ __forceinline__ R warp_sum(R v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -329,9 +373,23 @@ __device__ __forceinline__ void warp_sum4(R& a, R& b, R& c, R& d) {
     d = __shfl_sync(full, k, 24);
 }
 
-template <class R>
-__device__ __forceinline__ void load_tab(const R* __restrict__ tab, R* K, int n) {
-    for (int k = threadIdx.x; k < n; k += blockDim.x) K[k] = tab[k];
+// Global -> shared copy of n values by the block, U loads in flight per thread.
+template <int U, class R>
+__device__ __forceinline__ void copy_to_smem(const R* __restrict__ g, R* s, int n) {
+    const int bd = blockDim.x;
+    for (int k0 = threadIdx.x; k0 < n; k0 += U * bd) {
+        R v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int k = k0 + u * bd;
+            v[u] = k < n ? g[k] : (R)0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int k = k0 + u * bd;
+            if (k < n) s[k] = v[u];
+        }
+    }
 }
 
 // A flattened loop index k = i * B + j walked with a fixed stride S: (i, j) advance
@@ -410,7 +468,7 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     unsigned char* lofm = reinterpret_cast<unsigned char*>(lcnt + NS);  // L2
     unsigned short* ptab = reinterpret_cast<unsigned short*>(lofm + ((L2 + 1) & ~1));  // n_pairs: ia << 8 | jb
     const int tid = threadIdx.x, bd = blockDim.x;
-    load_tab(tab, K, tb.size);
+    copy_to_smem<4>(tab, K, tb.size);
     for (int k = tid; k < L2; k += bd) lofm[k] = (unsigned char)l_of_lm(k);
     const int NA4 = NMP / 4, items = NS * L2 * NA4;  // NA4 also sizes the transform's vector loads
 
@@ -439,10 +497,14 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     for (int base = p0; base < p1; base += TC) {
         const int cnt = min(TC, p1 - base);
         __syncthreads();
-        if (tid < 32) build_species_lists<TC>(sc, base, cnt, Z, nj, nd, spc, lst, lcnt);
-        else if (tid - 32 < cnt) {
-            const int t = tid - 32;
-            stage_neighbour<R>(sc, nd[base + t], dsm + DS * t, fcs + t, (R*)nullptr);
+        {
+            ChunkFetch nf;  // loaded where it is staged: registers are this kernel's occupancy limit
+            nf.load<TC>(base, p1, Z, nj, nd);
+            if (tid < 32) build_species_lists<TC>(sc, cnt, nf, spc, lst, lcnt);
+            else if (tid - 32 < cnt) {
+                const int t = tid - 32;
+                stage_neighbour<R>(sc, nf.d, dsm + DS * t, fcs + t, (R*)nullptr);
+            }
         }
         __syncthreads();
         // Ylm columns and radial rows of the staged neighbours as one task list: first the
@@ -581,7 +643,8 @@ __host__ __device__ __forceinline__ BwdPlan bwd_plan(const SoapConst& sc) {
     BwdPlan p;
     p.hs = soap_tab(sc.n_max, L).size;
     p.U = p.hs + ((NS * L2 * NMP + 7) & ~7);
-    p.pre = 2 * sc.ncomp + sc.n_pairs * L;
+    const int NN = NS * sc.n_max, NNP = (NN + 1) & ~1;
+    p.pre = 2 * ((sc.ncomp + 3) & ~3) + L * NN * NNP;  // c, dE/dc, symmetric dE/dp matrices
     p.stage = 4 * TCB * L2 + 2 * TCB * L * NMP + (2 + DS) * TCB;
     p.ints_at = p.U + (((p.pre > p.stage ? p.pre : p.stage) + 7) & ~7);
     return p;
@@ -612,9 +675,10 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
     R* hs = K + pl.hs;                                  // NS * L2 * NMP
     R* U = K + pl.U;
     // pre-phase view of U
+    const int NNP = (NN + 1) & ~1;                      // row length of the dE/dp matrices (even)
     R* cs = U;                                          // ncomp
-    R* dc = cs + sc.ncomp;                              // ncomp
-    R* dp = dc + sc.ncomp;                              // np
+    R* dc = cs + ((sc.ncomp + 3) & ~3);                 // ncomp
+    R* Hf = dc + ((sc.ncomp + 3) & ~3);                 // L * NN * NNP: H_l[b][a] = dE/dp(pair(a, b), l)
     // staging view of U
     Dual<R>* Yd = reinterpret_cast<Dual<R>*>(U);        // TCB * L2
     R* Ism = U + 4 * TCB * L2;                          // TCB * L * NMP
@@ -626,15 +690,36 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
     int* lst = spc + TCB;                               // NS * TCB
     int* lcnt = lst + NS * TCB;                         // NS
     unsigned char* lofm = reinterpret_cast<unsigned char*>(lcnt + NS);  // L2
+    unsigned short* ptab = reinterpret_cast<unsigned short*>(lofm + ((L2 + 1) & ~1));  // n_pairs: ia << 8 | jb
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, bd = blockDim.x;
-    load_tab(tab, K, tb.size);
-    for (int k = tid; k < L2; k += bd) lofm[k] = (unsigned char)l_of_lm(k);
-    const R* cg = c_in + (size_t)ci * sc.ncomp;
-    for (int k = tid; k < sc.ncomp; k += bd) cs[k] = cg[k];
+    const int p0 = off[atom], p1 = off[atom + 1];
+    ChunkFetch nf;
+    if (p0 < p1) nf.load<TCB>(p0, p1, Z, nj, nd);
+    // q.G, the entries of this thread's first QU strides kept in registers for dE/dp
+    constexpr int QU = 8;
     const R* qg = q_in + (size_t)ci * sc.dpad;
     const R* gg = G + (size_t)ci * sc.dpad;
+    R qv[QU], gv[QU];
+#pragma unroll
+    for (int u = 0; u < QU; ++u) {
+        const int k = tid + u * bd;
+        qv[u] = k < np ? qg[k] : (R)0;
+        gv[u] = k < np ? gg[k] : (R)0;
+    }
+    copy_to_smem<4>(tab, K, tb.size);
+    copy_to_smem<8>(c_in + (size_t)ci * sc.ncomp, cs, sc.ncomp);
+    for (int k = tid; k < L2; k += bd) lofm[k] = (unsigned char)l_of_lm(k);
+    for (int pr = tid; pr < sc.n_pairs; pr += bd) {
+        int ia, jb;
+        decode_pair(pr, ia, jb);
+        ptab[pr] = (unsigned short)(ia << 8 | jb);
+    }
+    if (NNP > NN)
+        for (int k = tid; k < L * NN; k += bd) Hf[k * NNP + NN] = 0;
     R part = 0;
-    for (int k = tid; k < np; k += bd) part += qg[k] * gg[k];
+#pragma unroll
+    for (int u = 0; u < QU; ++u) part += qv[u] * gv[u];
+    for (int k = tid + QU * bd; k < np; k += bd) part += qg[k] * gg[k];
     __shared__ double s_wsum[BWD_WARPS];
     __shared__ R s_sc[2];
     __shared__ R s_f[3 * TCB];  // per-pair forces of the last chunk, flushed during the next staging
@@ -649,31 +734,35 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
     }
     __syncthreads();
     const R sq = s_sc[0], inv = s_sc[1];
-    for (int pr = tid; pr < sc.n_pairs; pr += bd) {
-        int ia, jb;
-        decode_pair(pr, ia, jb);
-        const R f0 = ia != jb ? (R)1.41421356237309504880 : (R)2;
-        for (int l = 0; l < L; ++l) {
-            const int k = pr * L + l;
-            const R v = sc.normalise ? (gg[k] - qg[k] * sq) * inv : gg[k];
-            dp[k] = v * f0 * K[tb.lf + l];
+    // dE/dp[pair * L + l] into the symmetric matrices H_l (both triangles)
+    {
+        Walk2 w(tid, bd, L);  // (pair, l) of k = tid + u * bd
+        auto put = [&](int pr, int l, R q, R g) {
+            const int ia = ptab[pr] >> 8, jb = ptab[pr] & 255;
+            const R f0 = ia != jb ? (R)1.41421356237309504880 : (R)2;
+            const R v = (sc.normalise ? (g - q * sq) * inv : g) * f0 * K[tb.lf + l];
+            R* H = Hf + l * NN * NNP;
+            H[ia * NNP + jb] = v;
+            H[jb * NNP + ia] = v;
+        };
+#pragma unroll
+        for (int u = 0; u < QU; ++u) {
+            if (tid + u * bd < np) put(w.i, w.j, qv[u], gv[u]);
+            w.next();
         }
+        for (int k = tid + QU * bd; k < np; k += bd, w.next()) put(w.i, w.j, qg[k], gg[k]);
     }
     __syncthreads();
-    if (tid < sc.ncomp) {
-        Walk2 w(tid, bd, L2);
-        for (; w.i < NN; w.next()) {
-            const int a = w.i, lm = w.j, l = lofm[lm];
-            R acc = 0;
-            int idx = (a * (a + 1) / 2) * L + l;  // pair (a, b = 0)
-            const R* cb = cs + lm;
-            for (int b = 0; b <= a; ++b, idx += L) acc += dp[idx] * cb[b * L2];
-            idx = ((a + 1) * (a + 2) / 2 + a) * L + l;  // pair (b = a + 1, a)
-            for (int b = a + 1; b < NN; ++b) {
-                acc += dp[idx] * cb[b * L2];
-                idx += (b + 1) * L;
-            }
-            dc[a * L2 + lm] = acc;
+    // dE/dc[a][lm] = sum_b H_l[b][a] c[b][lm], rows a and a + 1 per thread; the row pair
+    // is fastest, so a warp reads few distinct c and consecutive H entries
+    {
+        Walk2 w(tid, bd, NNP / 2);
+        for (; w.i < L2; w.next()) {
+            const int lm = w.i, a = 2 * w.j;
+            R d0, d1;
+            hrow2(Hf + lofm[lm] * NN * NNP + a, cs + lm, NN, NNP, L2, d0, d1);
+            dc[a * L2 + lm] = d0;
+            if (a + 1 < NN) dc[(a + 1) * L2 + lm] = d1;
         }
     }
     __syncthreads();
@@ -699,15 +788,14 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
         }
     }
     const R alpha = (R)sc.alpha;
-    const int p0 = off[atom], p1 = off[atom + 1];
     int prev = p0, prev_cnt = 0;
     for (int base = p0; base < p1; base += TCB) {
         const int cnt = min(TCB, p1 - base);
         __syncthreads();
-        if (tid < 32) build_species_lists<TCB>(sc, base, cnt, Z, nj, nd, spc, lst, lcnt);
+        if (tid < 32) build_species_lists<TCB>(sc, cnt, nf, spc, lst, lcnt);
         else if (tid - 32 < cnt) {
             const int t = tid - 32;
-            stage_neighbour<R>(sc, nd[base + t], dsm + DS * t, fcs + t, dfcs + t);
+            stage_neighbour<R>(sc, nf.d, dsm + DS * t, fcs + t, dfcs + t);
         } else if (tid >= 64 && tid - 64 < 3 * prev_cnt) {
             fpair[3 * (size_t)prev + (tid - 64)] += (double)s_f[tid - 64];
         }
@@ -724,6 +812,7 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
         prev = base;
         prev_cnt = cnt;
         __syncthreads();
+        if (base + TCB < p1) nf.load<TCB>(base + TCB, p1, Z, nj, nd);
         // one task list as in the forward kernel: Ylm columns (m descending, neighbour
         // fastest), then the radial rows (t, a) with their r-derivatives
         const int nY = cnt * L, nT = nY + cnt * nm;
@@ -805,7 +894,7 @@ template <class R>
 size_t bwd_smem(const SoapConst& sc) {
     const int L = sc.l_max + 1;
     return sizeof(R) * (size_t)bwd_plan(sc).ints_at + sizeof(int) * (TCB + sc.n_species * TCB + sc.n_species) +
-           (size_t)(L * L) + 64;
+           (size_t)((L * L + 1) & ~1) + 2 * (size_t)sc.n_pairs + 64;
 }
 
 template <class R, int FQ>
