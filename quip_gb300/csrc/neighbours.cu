@@ -200,68 +200,93 @@ __global__ void __launch_bounds__(128) k_pairs(int n, const double* __restrict__
     const double cutoff = g.cutoff;
     int count = 0;
     const int base = FILL ? off[a] : 0;
-    const unsigned lt = (1u << lane) - 1u;
-    for (int k2 = mn[2]; k2 <= mx[2]; ++k2) {
-        int t = cc[2] + k2;
-        int k3 = g.cellsN[2] > 1 ? ((t % g.cellsN[2]) + g.cellsN[2]) % g.cellsN[2] : 0;
-        int k4 = (t - k3) / g.cellsN[2];
-        for (int j2 = mn[1]; j2 <= mx[1]; ++j2) {
-            int u = cc[1] + j2;
-            int j3 = g.cellsN[1] > 1 ? ((u % g.cellsN[1]) + g.cellsN[1]) % g.cellsN[1] : 0;
-            int j4 = (u - j3) / g.cellsN[1];
-            for (int i2 = mn[0]; i2 <= mx[0]; ++i2) {
-                int v = cc[0] + i2;
-                int i3 = g.cellsN[0] > 1 ? ((v % g.cellsN[0]) + g.cellsN[0]) % g.cellsN[0] : 0;
-                int i4 = (v - i3) / g.cellsN[0];
-                const int cl_loc = i3 + g.cellsN[0] * (j3 + g.cellsN[1] * k3);
-                const int cl = g.cell_base + cl_loc;
-                const bool same_cell = (cl_loc == lin);
-                const float ox = g.lat32[0] * i4 + g.lat32[3] * j4 + g.lat32[6] * k4 - pa32.x;
-                const float oy = g.lat32[1] * i4 + g.lat32[4] * j4 + g.lat32[7] * k4 - pa32.y;
-                const float oz = g.lat32[2] * i4 + g.lat32[5] * j4 + g.lat32[8] * k4 - pa32.z;
-                const int e = cend[cl];
-                for (int q0 = cstart[cl]; q0 < e; q0 += 32) {
-                    const int q = q0 + lane;
-                    bool keep = false;
-                    int b = -1, s0 = 0, s1 = 0, s2 = 0;
-                    double d0 = 0, d1 = 0, d2 = 0, r = 0;
-                    if (q < e) {
-                        b = sorted[q];
-                        const float4 pb = wpos[q];
-                        float fx = pb.x + ox, fy = pb.y + oy, fz = pb.z + oz;
-                        const bool self0 = (b == a && i4 == 0 && j4 == 0 && k4 == 0 && same_cell);
-                        const float r2 = fx * fx + fy * fy + fz * fz;
-                        const bool sure = r2 < sure2;
-                        if (!FILL && sure && !self0) keep = true;
-                        else if (!self0 && r2 < lim2) {
-                            s0 = i4 - msa0 + ms[3 * b]; s1 = j4 - msa1 + ms[3 * b + 1]; s2 = k4 - msa2 + ms[3 * b + 2];
-                            if (MIXED && sure) {
-                                pair_vector_mixed(phi, plo, g, a, b, s0, s1, s2, d0, d1, d2, r);
-                                keep = true;
-                            } else {
-                                pair_vector(pos, g.lat, a, b, s0, s1, s2, d0, d1, d2, r);
-                                keep = sure || (!(d0 > cutoff || d1 > cutoff || d2 > cutoff) && r < cutoff);
-                            }
-                        }
+    const unsigned lt = (1u << lane) - 1u, full = 0xffffffffu;
+    // The image cells in (k, j, i) order, i fastest, 32 at a time: lane c holds cell c's
+    // range and offset; the candidates of the 32 cells, in cell order, are then taken 32
+    // at a time with every lane busy (the same pair order as a cell-by-cell walk).
+    const int nx = mx[0] - mn[0] + 1, ny = mx[1] - mn[1] + 1, ncell = nx * ny * (mx[2] - mn[2] + 1);
+    for (int c0 = 0; c0 < ncell; c0 += 32) {
+        const int c = c0 + lane;
+        int qb = 0, len = 0, shift = 0;
+        float ox = 0.f, oy = 0.f, oz = 0.f;
+        if (c < ncell) {
+            const int i2 = mn[0] + c % nx, j2 = mn[1] + (c / nx) % ny, k2 = mn[2] + c / (nx * ny);
+            const int t = cc[2] + k2, u = cc[1] + j2, v = cc[0] + i2;
+            const int k3 = g.cellsN[2] > 1 ? ((t % g.cellsN[2]) + g.cellsN[2]) % g.cellsN[2] : 0;
+            const int j3 = g.cellsN[1] > 1 ? ((u % g.cellsN[1]) + g.cellsN[1]) % g.cellsN[1] : 0;
+            const int i3 = g.cellsN[0] > 1 ? ((v % g.cellsN[0]) + g.cellsN[0]) % g.cellsN[0] : 0;
+            const int k4 = (t - k3) / g.cellsN[2], j4 = (u - j3) / g.cellsN[1], i4 = (v - i3) / g.cellsN[0];
+            const int cl_loc = i3 + g.cellsN[0] * (j3 + g.cellsN[1] * k3);
+            const int cl = g.cell_base + cl_loc;
+            ox = g.lat32[0] * i4 + g.lat32[3] * j4 + g.lat32[6] * k4 - pa32.x;
+            oy = g.lat32[1] * i4 + g.lat32[4] * j4 + g.lat32[7] * k4 - pa32.y;
+            oz = g.lat32[2] * i4 + g.lat32[5] * j4 + g.lat32[8] * k4 - pa32.z;
+            // cell shift in 10 bits per axis (|shift| <= img + 1 < 512) and the same-cell flag
+            shift = pack_shift(i4, j4, k4) | ((cl_loc == lin) ? (1 << 30) : 0);
+            const int q0 = cstart[cl];
+            len = cend[cl] - q0;
+            qb = q0;
+        }
+        int incl = len;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int x = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += x;
+        }
+        const int total = __shfl_sync(full, incl, 31);
+        qb -= incl - len;  // candidate f of this cell is sorted[qb + f]
+        for (int f0 = 0; f0 < total; f0 += 32) {
+            const int f = f0 + lane;
+            // owner cell: the number of cells whose candidates all precede f
+            int own = 0;
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int x = __shfl_sync(full, incl, own + step - 1);
+                if (x <= f) own += step;
+            }
+            own = min(own, 31);
+            const int q = __shfl_sync(full, qb, own) + f;
+            const int sh = __shfl_sync(full, shift, own);
+            const float fox = __shfl_sync(full, ox, own), foy = __shfl_sync(full, oy, own),
+                        foz = __shfl_sync(full, oz, own);
+            bool keep = false;
+            int b = -1, s0 = 0, s1 = 0, s2 = 0;
+            double d0 = 0, d1 = 0, d2 = 0, r = 0;
+            if (f < total) {
+                const int i4 = (sh & 1023) - 512, j4 = ((sh >> 10) & 1023) - 512, k4 = ((sh >> 20) & 1023) - 512;
+                const bool same_cell = (sh >> 30) & 1;
+                b = sorted[q];
+                const float4 pb = wpos[q];
+                float fx = pb.x + fox, fy = pb.y + foy, fz = pb.z + foz;
+                const bool self0 = (b == a && i4 == 0 && j4 == 0 && k4 == 0 && same_cell);
+                const float r2 = fx * fx + fy * fy + fz * fz;
+                const bool sure = r2 < sure2;
+                if (!FILL && sure && !self0) keep = true;
+                else if (!self0 && r2 < lim2) {
+                    s0 = i4 - msa0 + ms[3 * b]; s1 = j4 - msa1 + ms[3 * b + 1]; s2 = k4 - msa2 + ms[3 * b + 2];
+                    if (MIXED && sure) {
+                        pair_vector_mixed(phi, plo, g, a, b, s0, s1, s2, d0, d1, d2, r);
+                        keep = true;
+                    } else {
+                        pair_vector(pos, g.lat, a, b, s0, s1, s2, d0, d1, d2, r);
+                        keep = sure || (!(d0 > cutoff || d1 > cutoff || d2 > cutoff) && r < cutoff);
                     }
-                    const unsigned m = __ballot_sync(0xffffffffu, keep);
-                    if (FILL && keep) {
-                        const int p = base + count + __popc(m & lt);
-                        nj[p] = b;
-                        if (CALLER_LAYOUT) {
-                            ns[3 * (size_t)p] = s0;
-                            ns[3 * (size_t)p + 1] = s1;
-                            ns[3 * (size_t)p + 2] = s2;
-                        } else {
-                            nd[p] = make_double4(d0, d1, d2, r);
-                            ns[p] = pack_shift(s0, s1, s2);
-                            ni[p] = a;
-                        }
-                        if (r < 1e-10) atomicOr(bad, 2);
-                    }
-                    count += __popc(m);
                 }
             }
+            const unsigned m = __ballot_sync(full, keep);
+            if (FILL && keep) {
+                const int p = base + count + __popc(m & lt);
+                nj[p] = b;
+                if (CALLER_LAYOUT) {
+                    ns[3 * (size_t)p] = s0;
+                    ns[3 * (size_t)p + 1] = s1;
+                    ns[3 * (size_t)p + 2] = s2;
+                } else {
+                    nd[p] = make_double4(d0, d1, d2, r);
+                    ns[p] = pack_shift(s0, s1, s2);
+                    ni[p] = a;
+                }
+                if (r < 1e-10) atomicOr(bad, 2);
+            }
+            count += __popc(m);
         }
     }
     if (!FILL && lane == 0) cnt[a] = count;
@@ -274,9 +299,21 @@ __global__ void k_reverse(long long P, const int* __restrict__ off, const int* _
     const int a = ni[p], b = nj[p], s = ns[p];
     const int s0 = (s & 1023) - 512, s1 = ((s >> 10) & 1023) - 512, s2 = ((s >> 20) & 1023) - 512;
     const int want = pack_shift(-s0, -s1, -s2);
+    // b's list in batches of 8 entries (the loads of a batch are in flight together)
     int found = -1;
-    for (int q = off[b]; q < off[b + 1]; ++q)
-        if (nj[q] == a && ns[q] == want) { found = q; break; }
+    const int q1 = off[b + 1];
+    for (int q0 = off[b]; q0 < q1 && found < 0; q0 += 8) {
+        int jv[8], sv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int q = q0 + u;
+            jv[u] = q < q1 ? nj[q] : -1;
+            sv[u] = q < q1 ? ns[q] : 0;
+        }
+#pragma unroll
+        for (int u = 7; u >= 0; --u)
+            if (jv[u] == a && sv[u] == want) found = q0 + u;
+    }
     rev[p] = found;
     if (found < 0) atomicOr(bad, 4);
 }
@@ -451,6 +488,8 @@ int geom_finish(GeomDev& g, int n, const double* mm) {
         }
         if ((long long)(2 * g.img[0] + 1) * (2 * g.img[1] + 1) * (2 * g.img[2] + 1) > 2000000LL)
             GG_FAIL(GAPGPU_ERR_ATOMS, "calc_connect: cutoff is too large for the cell (more than 2e6 periodic images)");
+        if (g.img[0] > 500 || g.img[1] > 500 || g.img[2] > 500)
+            GG_FAIL(GAPGPU_ERR_ATOMS, "calc_connect: cutoff is too large for the cell (more than 500 images along an axis)");
     }
     // FP32 pre-filter data: origin of the effective cell, FP32 lattice, margin
     {
