@@ -204,6 +204,12 @@ int evaluate(gapgpu_context& c, int precision, const int* d_mask, bool timed) {
         GG_CUDA(cudaMemsetAsync(c.eatom.p, 0, sizeof(double) * n, c.stream));
         const int saved = c.precision;
         c.precision = precision;
+        // the distance_2b coordinates run together, in one pass over the pairs, at the
+        // position of the first of them
+        std::vector<const Coordinate*> two_body;
+        for (const Coordinate& co : m.coords)
+            if (co.type != DESC_SOAP) two_body.push_back(&co);
+        bool two_body_done = false;
         for (int k = 0; k < (int)m.coords.size() && !rc; ++k) {
             const Coordinate& co = m.coords[k];
             if (co.type == DESC_SOAP) {
@@ -216,9 +222,10 @@ int evaluate(gapgpu_context& c, int precision, const int* d_mask, bool timed) {
                 if (rc) break;
                 record(c, timed);
                 if ((rc = soap_backward(c, co, n, nc))) break;
-            } else {
+            } else if (!two_body_done) {
+                two_body_done = true;
                 record(c, timed);
-                if ((rc = pair_2b(c, co, n, d_mask))) break;
+                if ((rc = pair_2b(c, two_body, d_mask))) break;
             }
         }
         c.precision = saved;
@@ -330,6 +337,7 @@ void compute_timings(gapgpu_context& c) {
             return ms;
         };
         int i = 1;
+        bool two_body_done = false;
         t.reduce += el(c.cev[0], c.cev[1]);  // output zeroing
         for (const Coordinate& co : c.model->coords) {
             if (co.type == DESC_SOAP) {
@@ -338,7 +346,8 @@ void compute_timings(gapgpu_context& c) {
                 t.gemm += el(c.cev[i + 1], c.cev[i + 2]);
                 t.soap_bwd += el(c.cev[i + 2], c.cev[i + 3]);
                 i += 3;
-            } else {
+            } else if (!two_body_done) {
+                two_body_done = true;
                 if (i + 1 >= c.ncev) break;
                 t.pair2b += el(c.cev[i], c.cev[i + 1]);
                 i += 1;

@@ -115,6 +115,6 @@ int select_centres(gapgpu_context& c, const Coordinate& co, int n, const int* d_
 int gp_fp64(gapgpu_context& c, const Coordinate& co, int nc);
 int gp_mixed(gapgpu_context& c, const Coordinate& co, int nc, int precision);
 // pair.cu
-int pair_2b(gapgpu_context& c, const Coordinate& co, int n, const int* d_mask);
+int pair_2b(gapgpu_context& c, const std::vector<const Coordinate*>& coords, const int* d_mask);
 int gather_outputs(gapgpu_context& c, const gapgpu_model& m, int n, const int* d_mask);
 }  // namespace gapgpu

@@ -15,6 +15,9 @@
 //   F_a   = sum_{p in a} (f_p - f_rev(p))
 //   W_a   = sum_{p in a} d_p (x) f_rev(p)
 //   e_a   = eatom_a + sum_{p in a} (epair_p + epair_rev(p)) + e0(Z_a) [mask]
+#include <algorithm>
+#include <vector>
+
 #include "context.h"
 
 namespace gapgpu {
@@ -38,16 +41,28 @@ __device__ __forceinline__ void fcut(R r, R rc, R w, R& f, R& df) {
     f = 1; df = 0;
 }
 
+// The distance_2b coordinates of a model, evaluated together in one pass over the pairs.
+constexpr int MAX_2B = 16;
+struct Pair2bSet {
+    int n;
+    struct Entry {
+        double rc, w, it2;      // cutoff, transition width, 1 / theta^2
+        int Z1, Z2, M;
+        const void* X;          // [M] sparse points (R)
+        const void* coef;       // [M] alpha sparseCutoff delta^2 (R)
+    } c[MAX_2B];
+};
+
 // One thread per canonical directed pair (i < j, or i == j with the shift
-// lexicographically positive).  The reverse pair has the same r (bitwise) and hence the
-// same descriptor value, energy and opposite force, so it is written by the same thread:
-// every fpair/epair slot still has exactly one writer per descriptor.
+// lexicographically positive), all distance_2b coordinates of the set.  The reverse
+// pair has the same r (bitwise) and hence the same descriptor value, energy and
+// opposite force, so it is written by the same thread: every fpair/epair slot still has
+// exactly one writer.
 template <class R>
 __global__ void k_pair_2b(long long P, const int* __restrict__ Z, const int* __restrict__ mask, const int* __restrict__ ni,
                           const int* __restrict__ nj, const int* __restrict__ ns, const int* __restrict__ rev,
-                          const double4* __restrict__ nd, double rc, double w, int Z1, int Z2, int M,
-                          const R* __restrict__ X, const R* __restrict__ coef, double theta,
-                          double* __restrict__ fpair, double* __restrict__ epair) {
+                          const double4* __restrict__ nd, const Pair2bSet set, double* __restrict__ fpair,
+                          double* __restrict__ epair) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (p >= P) return;
     const int a = ni[p], b = nj[p];
@@ -58,27 +73,39 @@ __global__ void k_pair_2b(long long P, const int* __restrict__ Z, const int* __r
         if (!(s0 > 0 || (s0 == 0 && (s1 > 0 || (s1 == 0 && s2 > 0))))) return;
     }
     const double4 d = nd[p];
-    if (d.w >= rc) return;
-    const int za = Z[a], zb = Z[b];
-    const bool zi1 = Z1 == 0 || za == Z1, zj2 = Z2 == 0 || zb == Z2, zi2 = Z2 == 0 || za == Z2, zj1 = Z1 == 0 || zb == Z1;
-    if (!((zi1 && zj2) || (zi2 && zj1))) return;
     const bool ca = !mask || mask[a], cb = !mask || mask[b];
     if (!ca && !cb) return;
-    // FP64 path: every step in double; mixed path: FP32 GP sum and force, FP64 accumulation.
-    const R r = (R)d.w, it2 = (R)(1.0 / (theta * theta));
-    R e = 0, de = 0;
-    for (int s = 0; s < M; ++s) {
-        R t = r - X[s];
-        R k = coef[s] * exp(-(R)0.5 * t * t * it2);
-        e += k;
-        de -= k * t * it2;
+    const int za = Z[a], zb = Z[b];
+    // FP64 path: every step in double; mixed path: FP32 GP sums and force, FP64 accumulation.
+    const R r = (R)d.w;
+    R g = 0, ef = 0;
+    bool any = false;
+    for (int k = 0; k < set.n; ++k) {
+        const Pair2bSet::Entry& cd = set.c[k];
+        if (d.w >= cd.rc) continue;
+        const bool zi1 = cd.Z1 == 0 || za == cd.Z1, zj2 = cd.Z2 == 0 || zb == cd.Z2;
+        const bool zi2 = cd.Z2 == 0 || za == cd.Z2, zj1 = cd.Z1 == 0 || zb == cd.Z1;
+        if (!((zi1 && zj2) || (zi2 && zj1))) continue;
+        const R* X = static_cast<const R*>(cd.X);
+        const R* coef = static_cast<const R*>(cd.coef);
+        const R it2 = (R)cd.it2;
+        R e = 0, de = 0;
+        for (int s = 0; s < cd.M; ++s) {
+            const R t = r - X[s];
+            const R kv = coef[s] * exp(-(R)0.5 * t * t * it2);
+            e += kv;
+            de -= kv * t * it2;
+        }
+        R f, df;
+        fcut<R>(r, (R)cd.rc, (R)cd.w, f, df);
+        g += de * f + e * df;
+        ef += e * f;
+        any = true;
     }
-    R f, df;
-    fcut<R>(r, (R)rc, (R)w, f, df);
-    const R g = de * f + e * df;
+    if (!any) return;
     const R ir = (R)1 / r;
     const double fx = (double)(g * (R)d.x * ir), fy = (double)(g * (R)d.y * ir), fz = (double)(g * (R)d.z * ir);
-    const double h = 0.5 * (double)(e * f);
+    const double h = (double)((R)0.5 * ef);
     if (ca) {
         fpair[3 * (size_t)p] += fx; fpair[3 * (size_t)p + 1] += fy; fpair[3 * (size_t)p + 2] += fz;
         epair[p] += h;
@@ -167,25 +194,40 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_final(const int* __restr
 
 }  // namespace
 
-int pair_2b(gapgpu_context& c, const Coordinate& co, int n, const int* d_mask) {
-    (void)n;
-    if (co.cov != COV_ARD_SE) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "distance_2b needs the ard_se covariance");
+int pair_2b(gapgpu_context& c, const std::vector<const Coordinate*>& coords, const int* d_mask) {
+    for (const Coordinate* co : coords)
+        if (co->cov != COV_ARD_SE) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "distance_2b needs the ard_se covariance");
     const long long P = c.n_pairs;
-    if (P == 0) return GAPGPU_OK;
+    if (P == 0 || coords.empty()) return GAPGPU_OK;
+    const bool fp64 = c.precision == GAPGPU_FP64;
     const int TB = 256;
     const unsigned nb = (unsigned)((P + TB - 1) / TB);
-    if (c.precision == GAPGPU_FP64)
-        k_pair_2b<double><<<nb, TB, 0, c.stream>>>(P, c.Z.as<int>(), d_mask, c.nbr_i.as<int>(), c.nbr_j.as<int>(),
-                                                   c.nbr_s.as<int>(), c.nbr_rev.as<int>(), c.nbr_d.as<double4>(), co.d2_rc,
-                                                   co.d2_w, co.d2_Z1, co.d2_Z2, co.M, co.dX64, co.dcoef, co.theta[0],
-                                                   c.fpair.as<double>(), c.epair.as<double>());
-    else
-        k_pair_2b<float><<<nb, TB, 0, c.stream>>>(P, c.Z.as<int>(), d_mask, c.nbr_i.as<int>(), c.nbr_j.as<int>(),
-                                                  c.nbr_s.as<int>(), c.nbr_rev.as<int>(), c.nbr_d.as<double4>(), co.d2_rc,
-                                                  co.d2_w, co.d2_Z1, co.d2_Z2, co.M, co.dXf32, co.dcoef32, co.theta[0],
-                                                  c.fpair.as<double>(), c.epair.as<double>());
-    c.launches++;
-    GG_CUDA(cudaGetLastError());
+    for (size_t k0 = 0; k0 < coords.size(); k0 += MAX_2B) {
+        Pair2bSet set{};
+        set.n = (int)std::min<size_t>(MAX_2B, coords.size() - k0);
+        for (int k = 0; k < set.n; ++k) {
+            const Coordinate& co = *coords[k0 + k];
+            Pair2bSet::Entry& e = set.c[k];
+            e.rc = co.d2_rc;
+            e.w = co.d2_w;
+            e.it2 = 1.0 / (co.theta[0] * co.theta[0]);
+            e.Z1 = co.d2_Z1;
+            e.Z2 = co.d2_Z2;
+            e.M = co.M;
+            e.X = fp64 ? (const void*)co.dX64 : (const void*)co.dXf32;
+            e.coef = fp64 ? (const void*)co.dcoef : (const void*)co.dcoef32;
+        }
+        if (fp64)
+            k_pair_2b<double><<<nb, TB, 0, c.stream>>>(P, c.Z.as<int>(), d_mask, c.nbr_i.as<int>(), c.nbr_j.as<int>(),
+                                                       c.nbr_s.as<int>(), c.nbr_rev.as<int>(), c.nbr_d.as<double4>(), set,
+                                                       c.fpair.as<double>(), c.epair.as<double>());
+        else
+            k_pair_2b<float><<<nb, TB, 0, c.stream>>>(P, c.Z.as<int>(), d_mask, c.nbr_i.as<int>(), c.nbr_j.as<int>(),
+                                                      c.nbr_s.as<int>(), c.nbr_rev.as<int>(), c.nbr_d.as<double4>(), set,
+                                                      c.fpair.as<double>(), c.epair.as<double>());
+        c.launches++;
+        GG_CUDA(cudaGetLastError());
+    }
     return GAPGPU_OK;
 }
 
