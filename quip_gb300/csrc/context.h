@@ -6,6 +6,15 @@
 
 namespace gapgpu {
 
+#ifdef __CUDACC__
+// FP32 -> TF32 operand, round to nearest (ties away), low 13 mantissa bits zero
+__device__ __forceinline__ float round_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+#endif
+
 // A growable device buffer.
 struct DBuf {
     void* p = nullptr;

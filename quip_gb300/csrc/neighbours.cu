@@ -299,21 +299,9 @@ __global__ void k_reverse(long long P, const int* __restrict__ off, const int* _
     const int a = ni[p], b = nj[p], s = ns[p];
     const int s0 = (s & 1023) - 512, s1 = ((s >> 10) & 1023) - 512, s2 = ((s >> 20) & 1023) - 512;
     const int want = pack_shift(-s0, -s1, -s2);
-    // b's list in batches of 8 entries (the loads of a batch are in flight together)
     int found = -1;
-    const int q1 = off[b + 1];
-    for (int q0 = off[b]; q0 < q1 && found < 0; q0 += 8) {
-        int jv[8], sv[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int q = q0 + u;
-            jv[u] = q < q1 ? nj[q] : -1;
-            sv[u] = q < q1 ? ns[q] : 0;
-        }
-#pragma unroll
-        for (int u = 7; u >= 0; --u)
-            if (jv[u] == a && sv[u] == want) found = q0 + u;
-    }
+    for (int q = off[b]; q < off[b + 1]; ++q)
+        if (nj[q] == a && ns[q] == want) { found = q; break; }
     rev[p] = found;
     if (found < 0) atomicOr(bad, 4);
 }

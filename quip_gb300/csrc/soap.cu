@@ -445,7 +445,8 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
                                                                const int* __restrict__ centres, const int* __restrict__ Z,
                                                                const int* __restrict__ off, const int* __restrict__ nj,
                                                                const double4* __restrict__ nd, R* __restrict__ c_out,
-                                                               R* __restrict__ q_out, double* __restrict__ pnorm) {
+                                                               R* __restrict__ q_out, float* __restrict__ qr_out,
+                                                               double* __restrict__ pnorm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ci = blockIdx.x;
     if (ci >= nc) return;
@@ -621,12 +622,14 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     const R inv = s_inv;
     const int np = sc.n_pairs * L;
     R* qg = q_out + (size_t)ci * sc.dpad;
+    float* qrg = qr_out ? qr_out + (size_t)ci * sc.dpad : nullptr;  // TF32-rounded copy (GEMM operand)
     for (int k = tid; k < sc.dpad; k += bd) {
         R v;
         if (k < np) v = ps[k] * inv;
         else if (k == np) v = (R)sc.sigma0;
         else v = 0;
         qg[k] = v;
+        if (qrg) __stcs(qrg + k, round_tf32((float)v));
     }
 }
 
@@ -903,7 +906,9 @@ int launch_forward_fq(gapgpu_context& c, const Coordinate& co, int nc, const Soa
     const R* tab = static_cast<const R*>(co.dtab[sizeof(R) == 4 ? 1 : 0]);
     k_soap_forward<R, FQ><<<nc, FWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.cur_centres, c.Z.as<int>(), c.nbr_off.as<int>(),
                                                              c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.scratch.as<R>(),
-                                                             c.qbuf.as<R>(), c.pnorm.as<double>());
+                                                             c.qbuf.as<R>(),
+                                                             c.precision == GAPGPU_MIXED_TF32 ? c.qlo.as<float>() : nullptr,
+                                                             c.pnorm.as<double>());
     c.launches++;
     GG_CUDA(cudaGetLastError());
     return GAPGPU_OK;
@@ -1011,6 +1016,7 @@ int soap_forward(gapgpu_context& c, const Coordinate& co, int n, int nc) {
     if ((rc = c.scratch.ensure(rs * (size_t)nc * sc.ncomp)) || (rc = c.qbuf.ensure(rs * (size_t)nc * sc.dpad)) ||
         (rc = c.pnorm.ensure(sizeof(double) * nc)))
         return rc;
+    if (c.precision == GAPGPU_MIXED_TF32 && (rc = c.qlo.ensure(sizeof(float) * (size_t)nc * sc.dpad))) return rc;
     if (nc == 0) return GAPGPU_OK;
     return mixed ? launch_forward<float>(c, co, nc) : launch_forward<double>(c, co, nc);
 }

@@ -180,12 +180,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ float round_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
-}
-
 struct EpiParams {
     int rows;             // valid rows (centres)
     int ldo;              // leading dimension of the outputs
@@ -378,10 +372,6 @@ __global__ void k_split_q(size_t n, const float* __restrict__ q, __nv_bfloat16* 
     __nv_bfloat16 h = __float2bfloat16_rn(x);
     hi[i] = h;
     lo[i] = __float2bfloat16_rn(x - __bfloat162float(h));
-}
-__global__ void k_round_q(size_t n, const float* __restrict__ q, float* __restrict__ out) {
-    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i < n) out[i] = round_tf32(q[i]);
 }
 __global__ void k_rowsum_scatter32(int nc, int ntiles, const double* __restrict__ epart, const int* __restrict__ centres,
                                    double* __restrict__ eatom) {
@@ -596,11 +586,11 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
     int* err = c.total.as<int>() + 3;  // cleared at the start of the evaluation, read after it
     const int TB = 256;
     const unsigned nb = (unsigned)((nq + TB - 1) / TB);
-    if (MODE == MODE_BF16X3)
+    // TF32: the forward kernel wrote the rounded descriptors to qlo next to q
+    if (MODE == MODE_BF16X3) {
         k_split_q<<<nb, TB, 0, c.stream>>>(nq, c.qbuf.as<float>(), c.Kbuf.as<__nv_bfloat16>(), c.qlo.as<__nv_bfloat16>());
-    else
-        k_round_q<<<nb, TB, 0, c.stream>>>(nq, c.qbuf.as<float>(), c.qlo.as<float>());
-    c.launches++;
+        c.launches++;
+    }
     const double z = co.zeta;
     EpiParams ep{nc, Mp, co.dcoef32, (float)z, (z == std::floor(z) && z >= 1 && z <= 64) ? (int)z : 0, c.Wbuf.p, c.Wlo.p,
                  c.epart.as<double>(), 0};
