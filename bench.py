@@ -241,6 +241,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serving-loads", default="500,1500,4000", help="offered loads (requests/s)")
     ap.add_argument("--serving-seconds", type=float, default=3.0)
+    ap.add_argument("--gemm-pairs", type=int, default=1, choices=[0, 1, 2],
+                    help="CTA-pair GEMM tiles: 0 off, 1 autotuner candidates, 2 only")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -321,6 +323,7 @@ def main():
                     F=d_F.cpu().numpy(), V=d_V.cpu().numpy().reshape(3, 3, order="F"))
 
     pot = Potential(param_filename=path, precision=args.precision)
+    pot.set_option("pairs", args.gemm_pairs)
     clk = Clocks(os.path.join(tmp, "clocks.csv"))
     with clk:
         t_wall0 = time.perf_counter()

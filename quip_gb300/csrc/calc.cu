@@ -472,6 +472,10 @@ int gapgpu_context_set_option(gapgpu_context* c, const char* key, int value) {
     if (k == "graphs") c->graph_mode = value ? 1 : 0;
     else if (k == "timing") c->timed = value != 0;
     else if (k == "autotune") c->autotune = value != 0;
+    else if (k == "pairs") {
+        if (value < 0 || value > 2) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_set_option: pairs must be 0, 1 or 2");
+        c->gemm_pairs = value;
+    }
     else if (k == "priority") {
         // the context's own stream, recreated at the device's highest (value != 0) or
         // default scheduling priority: kernels of higher-priority streams get free SMs first

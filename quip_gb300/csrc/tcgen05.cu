@@ -365,6 +365,192 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 }
 
+// ---------------------------------------------------------------- CTA pairs (TF32)
+// The same GEMM on 256-row tiles computed by a cluster of two CTAs (tcgen05
+// cta_group::2): each CTA loads its 128 rows of A and half of the BN rows of B, the
+// leader (cluster rank 0) issues one 256 x BN x 8 MMA per k-step that reads both CTAs'
+// shared memory and writes each CTA's accumulator rows into that CTA's TMEM.  Per SM the
+// shared-memory operand traffic per MAC drops from (128 + BN) to (128 + BN / 2) rows.
+//   full[s]   leader only: both CTAs' TMA loads complete on it (expect-tx of both)
+//   empty[s]  both: the leader's commit arrives on the pair (multicast)
+//   tfull[b]  both: accumulator buffer b ready (multicast commit)
+//   tempty[b] leader only: 4 epilogue warps of each CTA arrive (remote for the peer)
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release;\n barrier.cluster.wait.acquire;" ::: "memory");
+}
+// shared::cluster address of the same shared-memory location in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t mapa_rank(uint32_t saddr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t caddr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(caddr) : "memory");
+}
+__device__ __forceinline__ void tma_load_pair(void* dst, const CUtensorMap* tm, int c0, int c1, uint32_t bar_cluster,
+                                              uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], "
+        "[%1, {%2, %3}], [%4], %5;" ::"r"(su32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(bar_cluster), "l"(policy)
+        : "memory");
+}
+template <int BN>
+__device__ __forceinline__ constexpr uint32_t idesc_pair() {
+    // as idesc<MODE_TF32, BN> with M = 256 (bits 24-28: M >> 4)
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+}
+template <int BN>
+__device__ __forceinline__ void mma_pair(uint32_t dt, uint64_t a, uint64_t b, uint32_t acc) {
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
+                 "l"(a), "l"(b), "r"(idesc_pair<BN>()), "r"(acc));
+}
+__device__ __forceinline__ void commit_pair_multicast(uint64_t* bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(su32(bar)),
+        "h"((uint16_t)3)
+        : "memory");
+}
+__device__ __forceinline__ void commit_pair(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar)) : "memory");
+}
+
+template <int BN>
+struct PairCfg {
+    static constexpr int TILE_A = BM * 128;        // this CTA's 128 rows of A, 32 FP32 of K
+    static constexpr int TILE_B = (BN / 2) * 128;  // this CTA's half of the BN rows of B
+    static constexpr int STAGE = TILE_A + TILE_B;
+    static constexpr int STAGES = SMEM_BUDGET / STAGE > 8 ? 8 : SMEM_BUDGET / STAGE;
+    static_assert(STAGES >= 2, "stage ring too small");
+};
+
+// C[m, n] = sum_k A[m, k] B[n, k] over m_tiles (of 256 rows) x n_tiles output tiles.
+template <int EPI, int BN>
+__global__ void __launch_bounds__(THREADS, 1)
+    k_tc_gemm_pair(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, int m_tiles, int n_tiles,
+                   int kchunks, EpiParams ep, int* err) {
+    using C = PairCfg<BN>;
+    constexpr int S = C::STAGES;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t full[S], empty[S], tfull[2], tempty[2], drain;
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int abort_flag;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_rank();
+    const bool leader = rank == 0;
+    const int pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
+    const int ntiles = m_tiles * n_tiles;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 8); }
+        mbar_init(&drain, 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {  // one warp of each CTA: the pair's TMEM, the same columns in both
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_base)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    }
+    fence_before();
+    cluster_sync_all();  // barriers of both CTAs initialised before any cross-CTA signal
+    fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------- TMA producer (both CTAs)
+        const uint64_t pol_a = policy_evict_first(), pol_b = policy_evict_last();
+        int it = 0;
+        bool ok = true;
+        for (int tile = pair; tile < ntiles && ok; tile += npairs) {
+            const int m0 = (tile / n_tiles) * (2 * BM) + (int)rank * BM;
+            const int n0 = (tile % n_tiles) * BN + (int)rank * (BN / 2);
+            for (int kc = 0; kc < kchunks; ++kc, ++it) {
+                const int s = it % S;
+                if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1, &abort_flag, err, 1)) { ok = false; break; }
+                unsigned char* st = smem + (size_t)s * C::STAGE;
+                const uint32_t fb = mapa_rank(su32(&full[s]), 0);
+                if (leader) mbar_expect_tx(&full[s], 2 * C::STAGE);
+                const int kx = kc * 32;
+                tma_load_pair(st, &tA, kx, m0, fb, pol_a);
+                tma_load_pair(st + C::TILE_A, &tB, kx, n0, fb, pol_b);
+            }
+        }
+        if (!ok) {  // let the loads already issued land before the CTA exits
+            for (int j = it - 1; j >= 0 && j >= it - S; --j) {
+                if (leader) mbar_wait(&full[j % S], (j / S) & 1, &abort_flag, err, 0);
+                else mbar_wait(&empty[j % S], (j / S) & 1, &abort_flag, err, 0);
+            }
+        }
+    } else if (warp == 1 && lane == 0 && leader) {
+        // ---------------- MMA issuer (leader CTA)
+        int it = 0, t = 0;
+        bool ok = true;
+        for (int tile = pair; tile < ntiles && ok; tile += npairs, ++t) {
+            const int buf = t & 1;
+            if (t >= 2 && !mbar_wait(&tempty[buf], ((t >> 1) - 1) & 1, &abort_flag, err, 2)) break;
+            fence_after();
+            const uint32_t acc_addr = tmem + buf * ACC_STRIDE;
+            for (int kc = 0; kc < kchunks; ++kc, ++it) {
+                const int s = it % S;
+                if (!mbar_wait(&full[s], (it / S) & 1, &abort_flag, err, 2)) { ok = false; break; }
+                fence_after();
+                const uint32_t base = su32(smem + (size_t)s * C::STAGE);
+                const uint32_t bbase = base + C::TILE_A;
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    const uint32_t koff = kk * 32;  // 32 bytes (8 TF32) of K per instruction
+                    mma_pair<BN>(acc_addr, sdesc(base + koff), sdesc(bbase + koff), (kc > 0 || kk > 0) ? 1u : 0u);
+                }
+                commit_pair_multicast(&empty[s]);
+            }
+            if (ok) commit_pair_multicast(&tfull[buf]);
+        }
+        commit_pair(&drain);  // arrives once every MMA issued above has completed
+        mbar_wait(&drain, 0, &abort_flag, err, 0);
+    } else if (warp >= 2) {
+        // ---------------- epilogue (both CTAs; warps 2-5, TMEM lane quarter = warp % 4)
+        const int q = warp & 3;
+        const uint32_t te0 = mapa_rank(su32(&tempty[0]), 0), te1 = mapa_rank(su32(&tempty[1]), 0);
+        int t = 0;
+        for (int tile = pair; tile < ntiles; tile += npairs, ++t) {
+            const int buf = t & 1;
+            const int m0 = (tile / n_tiles) * (2 * BM) + (int)rank * BM, n0 = (tile % n_tiles) * BN;
+            if (!mbar_wait(&tfull[buf], (t >> 1) & 1, &abort_flag, err, 4)) break;
+            fence_after();
+            const int row = m0 + q * 32 + lane;
+            float e_acc = 0.f;
+#pragma unroll 1
+            for (int cc = 0; cc < BN / 32; ++cc) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_STRIDE + cc * 32, v);
+                if (row < ep.rows) epilogue_chunk<MODE_TF32, EPI>(ep, row, n0 + cc * 32, v, e_acc);
+                if constexpr (EPI == EPI_KERNEL) {
+                    if (cc & 1) {
+                        if (row < ep.rows) ep.epart[(size_t)row * ep.ntiles + (n0 + cc * 32) / 64] = (double)e_acc;
+                        e_acc = 0.f;
+                    }
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_cluster(buf ? te1 : te0);
+        }
+    }
+    fence_before();
+    cluster_sync_all();  // no CTA leaves while its pair may still read its shared memory or TMEM
+    if (warp == 1) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
 __global__ void k_split_q(size_t n, const float* __restrict__ q, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -458,14 +644,15 @@ int pick_bn(int MODE, int N) {
 // the timing loop of IP_setup_parallel (src/Potentials/IP.f95:1092-1134) applied to
 // tile shapes.  Inside a stream capture no timing is possible: the heuristic decides.
 struct TuneKey {
-    int mode, epi, N, K, rb;
+    int mode, epi, N, K, rb, pairs;
     bool operator<(const TuneKey& o) const {
-        return std::tie(mode, epi, N, K, rb) < std::tie(o.mode, o.epi, o.N, o.K, o.rb);
+        return std::tie(mode, epi, N, K, rb, pairs) < std::tie(o.mode, o.epi, o.N, o.K, o.rb, o.pairs);
     }
 };
+// A tile choice: BN > 0 one CTA per 128-row tile, BN < 0 a CTA pair per 256-row tile of -BN columns.
 struct TuneEntry {
     int bn;
-    std::vector<std::pair<int, float>> timings;  // (BN, ms)
+    std::vector<std::pair<int, float>> timings;  // (tile choice, ms)
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneEntry> g_tune;
@@ -476,13 +663,53 @@ int rows_bucket(int rows) {
     return b;
 }
 
+// pairs: 0 single-CTA tiles only, 1 also CTA-pair tiles (TF32), 2 CTA-pair tiles only
 template <int MODE>
-std::vector<int> bn_candidates(int N) {
+std::vector<int> bn_candidates(int N, int pairs) {
     std::vector<int> c;
-    if (N % 256 == 0 && Cfg<MODE, 256>::STAGES >= 2) c.push_back(256);
-    if (N % 192 == 0 && Cfg<MODE, 192>::STAGES >= 2) c.push_back(192);
-    c.push_back(128);
+    if (MODE != MODE_TF32) pairs = 0;
+    if (pairs < 2) {
+        if (N % 256 == 0 && Cfg<MODE, 256>::STAGES >= 2) c.push_back(256);
+        if (N % 192 == 0 && Cfg<MODE, 192>::STAGES >= 2) c.push_back(192);
+        c.push_back(128);
+    }
+    if (pairs >= 1) {
+        if (N % 256 == 0) c.push_back(-256);
+        if (N % 192 == 0) c.push_back(-192);
+        c.push_back(-128);
+    }
     return c;
+}
+
+template <int EPI, int BN>
+int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, int rows, int N, int kchunks, EpiParams ep,
+                int* err) {
+    using Cf = PairCfg<BN>;
+    const int smem = Cf::STAGES * Cf::STAGE + 1024;
+    GG_CUDA(cudaFuncSetAttribute(k_tc_gemm_pair<EPI, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const int m_tiles = (rows + 2 * BM - 1) / (2 * BM), n_tiles = N / BN;
+    if (EPI == EPI_KERNEL) ep.ntiles = N / 64;  // energy blocks of 64 columns
+    const int ntiles = m_tiles * n_tiles;
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = c.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    // persistent: as many pairs as can be resident at once (clusters stay within a GPC)
+    cfg.gridDim = dim3(2 * (num_sms() / 2));
+    int resident = 0;
+    GG_CUDA(cudaOccupancyMaxActiveClusters(&resident, k_tc_gemm_pair<EPI, BN>, &cfg));
+    const int npairs = std::max(1, std::min(ntiles, resident > 0 ? resident : num_sms() / 2));
+    cfg.gridDim = dim3(2 * npairs);
+    GG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_gemm_pair<EPI, BN>, a, b, m_tiles, n_tiles, kchunks, ep, err));
+    c.launches++;
+    return GAPGPU_OK;
 }
 
 template <int MODE, int EPI, int BN>
@@ -506,6 +733,11 @@ int launch_bn(gapgpu_context& c, const CUtensorMap& a0, const CUtensorMap& a1, c
 template <int MODE, int EPI>
 int launch_any(gapgpu_context& c, int BN, const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
                const CUtensorMap& b1, int rows, int N, int kchunks, const EpiParams& ep, int* err) {
+    if constexpr (MODE == MODE_TF32) {
+        if (BN == -256) return launch_pair<EPI, 256>(c, a0, b0, rows, N, kchunks, ep, err);
+        if (BN == -192) return launch_pair<EPI, 192>(c, a0, b0, rows, N, kchunks, ep, err);
+        if (BN == -128) return launch_pair<EPI, 128>(c, a0, b0, rows, N, kchunks, ep, err);
+    }
     if (BN == 256) return launch_bn<MODE, EPI, 256>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
     if (BN == 192) return launch_bn<MODE, EPI, 192>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
     return launch_bn<MODE, EPI, 128>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
@@ -522,16 +754,19 @@ int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows
     int rc;
     auto maps = [&](int BN, CUtensorMap& a0, CUtensorMap& a1, CUtensorMap& b0, CUtensorMap& b1) {
         int r;
-        if ((r = make_map(&a0, a0p, dt, es, K, rows, KB)) || (r = make_map(&b0, b0p, dt, es, K, N, KB, BN))) return r;
+        // a CTA pair loads half of the B tile in each CTA
+        const uint32_t bbox = BN > 0 ? (uint32_t)BN : (uint32_t)(-BN / 2);
+        if ((r = make_map(&a0, a0p, dt, es, K, rows, KB)) || (r = make_map(&b0, b0p, dt, es, K, N, KB, bbox))) return r;
         if (MODE == MODE_BF16X3) {
-            if ((r = make_map(&a1, a1p, dt, es, K, rows, KB)) || (r = make_map(&b1, b1p, dt, es, K, N, KB, BN))) return r;
+            if ((r = make_map(&a1, a1p, dt, es, K, rows, KB)) || (r = make_map(&b1, b1p, dt, es, K, N, KB, bbox))) return r;
         } else {
             a1 = a0;
             b1 = b0;
         }
         return (int)GAPGPU_OK;
     };
-    const TuneKey key{MODE, EPI, N, K, rows_bucket(rows)};
+    const int pairs = MODE == MODE_TF32 ? c.gemm_pairs : 0;
+    const TuneKey key{MODE, EPI, N, K, rows_bucket(rows), pairs};
     int BN = 0;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -546,7 +781,7 @@ int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows
         GG_CUDA(cudaEventCreate(&e0));
         GG_CUDA(cudaEventCreate(&e1));
         float best = 1e30f;
-        for (int bn : bn_candidates<MODE>(N)) {
+        for (int bn : bn_candidates<MODE>(N, pairs)) {
             CUtensorMap a0, a1, b0, b1;
             if ((rc = maps(bn, a0, a1, b0, b1))) return rc;
             if ((rc = launch_any<MODE, EPI>(c, bn, a0, a1, b0, b1, rows, N, kchunks, ep, err))) return rc;  // warm
@@ -565,7 +800,7 @@ int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune[key] = te;
     }
-    if (!BN) BN = pick_bn(MODE, N);
+    if (!BN) BN = pairs == 2 ? -(N % 192 == 0 ? 192 : 128) : pick_bn(MODE, N);
     CUtensorMap a0, a1, b0, b1;
     if ((rc = maps(BN, a0, a1, b0, b1))) return rc;
     if (ntiles_out) *ntiles_out = N / 64;
@@ -676,6 +911,10 @@ int gp_mixed(gapgpu_context& c, const Coordinate& co, int nc, int precision) {
 
 }  // namespace gapgpu
 
+namespace {
+std::string tile_name(int bn) { return bn > 0 ? std::to_string(bn) : "2x" + std::to_string(-bn); }
+}  // namespace
+
 extern "C" int gapgpu_tuning_report(char* buf, int capacity) {
     using namespace gapgpu;
     std::string out;
@@ -684,10 +923,11 @@ extern "C" int gapgpu_tuning_report(char* buf, int capacity) {
         const TuneKey& k = kv.first;
         out += std::string(k.mode == MODE_BF16X3 ? "bf16x3" : "tf32") + (k.epi == EPI_KERNEL ? " kernel" : " store") +
                " N=" + std::to_string(k.N) + " K=" + std::to_string(k.K) + " rows<=2^" + std::to_string(k.rb) +
-               " BN=" + std::to_string(kv.second.bn) + " [";
+               " BN=" + tile_name(kv.second.bn) + " [";
         for (size_t i = 0; i < kv.second.timings.size(); ++i) {
-            char t[48];
-            std::snprintf(t, sizeof t, "%s%d:%.3fms", i ? " " : "", kv.second.timings[i].first, kv.second.timings[i].second);
+            char t[64];
+            std::snprintf(t, sizeof t, "%s%s:%.3fms", i ? " " : "", tile_name(kv.second.timings[i].first).c_str(),
+                          kv.second.timings[i].second);
             out += t;
         }
         out += "]\n";
