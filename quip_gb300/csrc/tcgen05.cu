@@ -400,15 +400,13 @@ __device__ __forceinline__ void tma_load_pair(void* dst, const CUtensorMap* tm, 
         "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(bar_cluster), "l"(policy)
         : "memory");
 }
-template <int BN>
-__device__ __forceinline__ constexpr uint32_t idesc_pair() {
-    // as idesc<MODE_TF32, BN> with M = 256 (bits 24-28: M >> 4)
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+// as idesc<MODE_TF32, n> with M = 256 (bits 24-28: M >> 4); the tile width n is a run-time value
+__device__ __forceinline__ uint32_t idesc_pair(int n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
 }
-template <int BN>
-__device__ __forceinline__ void mma_pair(uint32_t dt, uint64_t a, uint64_t b, uint32_t acc) {
+__device__ __forceinline__ void mma_pair(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
     asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
-                 "l"(a), "l"(b), "r"(idesc_pair<BN>()), "r"(acc));
+                 "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void commit_pair_multicast(uint64_t* bar) {
     asm volatile(
@@ -429,11 +427,14 @@ struct PairCfg {
     static_assert(STAGES >= 2, "stage ring too small");
 };
 
-// C[m, n] = sum_k A[m, k] B[n, k] over m_tiles (of 256 rows) x n_tiles output tiles.
+// C[m, n] = sum_k A[m, k] B[n, k] over m_tiles (of 256 rows) x n_tiles output tiles of BN
+// columns; the last tile of a row block is N - (n_tiles - 1) BN wide (a multiple of 32):
+// each CTA still loads BN / 2 rows of B (rows past N read as zero) and the MMA takes the
+// first width / 2 of them.
 template <int EPI, int BN>
 __global__ void __launch_bounds__(THREADS, 1)
     k_tc_gemm_pair(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, int m_tiles, int n_tiles,
-                   int kchunks, EpiParams ep, int* err) {
+                   int N, int kchunks, EpiParams ep, int* err) {
     using C = PairCfg<BN>;
     constexpr int S = C::STAGES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -470,7 +471,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         bool ok = true;
         for (int tile = pair; tile < ntiles && ok; tile += npairs) {
             const int m0 = (tile / n_tiles) * (2 * BM) + (int)rank * BM;
-            const int n0 = (tile % n_tiles) * BN + (int)rank * (BN / 2);
+            const int nb = (tile % n_tiles) * BN, width = min(BN, N - nb);
+            const int n0 = nb + (int)rank * (width / 2);
             for (int kc = 0; kc < kchunks; ++kc, ++it) {
                 const int s = it % S;
                 if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1, &abort_flag, err, 1)) { ok = false; break; }
@@ -497,6 +499,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (t >= 2 && !mbar_wait(&tempty[buf], ((t >> 1) - 1) & 1, &abort_flag, err, 2)) break;
             fence_after();
             const uint32_t acc_addr = tmem + buf * ACC_STRIDE;
+            const uint32_t id = idesc_pair(min(BN, N - (tile % n_tiles) * BN));
             for (int kc = 0; kc < kchunks; ++kc, ++it) {
                 const int s = it % S;
                 if (!mbar_wait(&full[s], (it / S) & 1, &abort_flag, err, 2)) { ok = false; break; }
@@ -506,7 +509,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk) {
                     const uint32_t koff = kk * 32;  // 32 bytes (8 TF32) of K per instruction
-                    mma_pair<BN>(acc_addr, sdesc(base + koff), sdesc(bbase + koff), (kc > 0 || kk > 0) ? 1u : 0u);
+                    mma_pair(acc_addr, sdesc(base + koff), sdesc(bbase + koff), id, (kc > 0 || kk > 0) ? 1u : 0u);
                 }
                 commit_pair_multicast(&empty[s]);
             }
@@ -522,12 +525,13 @@ __global__ void __launch_bounds__(THREADS, 1)
         for (int tile = pair; tile < ntiles; tile += npairs, ++t) {
             const int buf = t & 1;
             const int m0 = (tile / n_tiles) * (2 * BM) + (int)rank * BM, n0 = (tile % n_tiles) * BN;
+            const int width = min(BN, N - n0);
             if (!mbar_wait(&tfull[buf], (t >> 1) & 1, &abort_flag, err, 4)) break;
             fence_after();
             const int row = m0 + q * 32 + lane;
             float e_acc = 0.f;
 #pragma unroll 1
-            for (int cc = 0; cc < BN / 32; ++cc) {
+            for (int cc = 0; cc < width / 32; ++cc) {
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_STRIDE + cc * 32, v);
                 if (row < ep.rows) epilogue_chunk<MODE_TF32, EPI>(ep, row, n0 + cc * 32, v, e_acc);
@@ -673,8 +677,8 @@ std::vector<int> bn_candidates(int N, int pairs) {
         if (N % 192 == 0 && Cfg<MODE, 192>::STAGES >= 2) c.push_back(192);
         c.push_back(128);
     }
-    if (pairs >= 1) {
-        if (N % 256 == 0) c.push_back(-256);
+    if (pairs >= 1) {  // N is a multiple of 128: 256-wide pair tiles end in a 128-wide one
+        if (N >= 256) c.push_back(-256);
         if (N % 192 == 0) c.push_back(-192);
         c.push_back(-128);
     }
@@ -687,7 +691,7 @@ int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, i
     using Cf = PairCfg<BN>;
     const int smem = Cf::STAGES * Cf::STAGE + 1024;
     GG_CUDA(cudaFuncSetAttribute(k_tc_gemm_pair<EPI, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    const int m_tiles = (rows + 2 * BM - 1) / (2 * BM), n_tiles = N / BN;
+    const int m_tiles = (rows + 2 * BM - 1) / (2 * BM), n_tiles = (N + BN - 1) / BN;
     if (EPI == EPI_KERNEL) ep.ntiles = N / 64;  // energy blocks of 64 columns
     const int ntiles = m_tiles * n_tiles;
     cudaLaunchConfig_t cfg = {};
@@ -707,7 +711,7 @@ int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, i
     GG_CUDA(cudaOccupancyMaxActiveClusters(&resident, k_tc_gemm_pair<EPI, BN>, &cfg));
     const int npairs = std::max(1, std::min(ntiles, resident > 0 ? resident : num_sms() / 2));
     cfg.gridDim = dim3(2 * npairs);
-    GG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_gemm_pair<EPI, BN>, a, b, m_tiles, n_tiles, kchunks, ep, err));
+    GG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_gemm_pair<EPI, BN>, a, b, m_tiles, n_tiles, N, kchunks, ep, err));
     c.launches++;
     return GAPGPU_OK;
 }
@@ -800,7 +804,7 @@ int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune[key] = te;
     }
-    if (!BN) BN = pairs == 2 ? -(N % 192 == 0 ? 192 : 128) : pick_bn(MODE, N);
+    if (!BN) BN = pairs == 2 ? (N >= 256 ? -256 : -128) : pick_bn(MODE, N);
     CUtensorMap a0, a1, b0, b1;
     if ((rc = maps(BN, a0, a1, b0, b1))) return rc;
     if (ntiles_out) *ntiles_out = N / 64;

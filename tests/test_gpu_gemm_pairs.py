@@ -6,7 +6,7 @@ import pytest
 
 from quip_gb300 import models
 
-from helpers import sic_model
+from helpers import oracle_descriptor_fn, sic_model
 
 pytestmark = pytest.mark.gpu
 
@@ -16,6 +16,16 @@ def sic_gap(tmp_path_factory):
     return sic_model(tmp_path_factory.mktemp("sic_pairs"))
 
 
+@pytest.fixture(scope="module")
+def sic_gap_tails(tmp_path_factory):
+    # D = 276 and M = 300 pad to 384: both GEMMs end in a 128-wide tile after a 256-wide one
+    rng = np.random.default_rng(3)
+    structs = [models.random_triclinic(int(n), rng=rng) for n in (40, 48, 56, 64, 40, 48, 56, 64)]
+    path = str(tmp_path_factory.mktemp("sic_pairs_tail") / "sic_gap.xml")
+    return models.random_soap_gap(path, oracle_descriptor_fn, structs, n_max=5, l_max=4, cutoff=4.5, width=1.0,
+                                  atom_sigma=0.5, species=(14, 6), M=300, zeta=4.0, delta=1.0, with_2b=True, seed=3)
+
+
 def _pot(path, pairs):
     from quip_gb300.potential import Potential
     pot = Potential(param_filename=path, precision="tf32")
@@ -23,11 +33,12 @@ def _pot(path, pairs):
     return pot
 
 
-@pytest.mark.parametrize("n", [37, 300, 520])
-def test_pair_tiles_match_single_cta_tiles(sic_gap, n):
+@pytest.mark.parametrize("n,tails", [(37, False), (300, False), (520, False), (300, True)])
+def test_pair_tiles_match_single_cta_tiles(sic_gap, sic_gap_tails, n, tails):
+    path = sic_gap_tails if tails else sic_gap
     at = models.random_triclinic(n, rng=np.random.default_rng(100 + n))
-    ref = _pot(sic_gap, 0).calc(at, local_energy=True)
-    got = _pot(sic_gap, 2).calc(at, local_energy=True)
+    ref = _pot(path, 0).calc(at, local_energy=True)
+    got = _pot(path, 2).calc(at, local_energy=True)
     scale = max(1.0, np.abs(ref["force"]).max())
     assert abs(got["energy"] - ref["energy"]) <= 1e-6 * max(1.0, abs(ref["energy"]))
     assert np.abs(got["force"] - ref["force"]).max() <= 1e-5 * scale
