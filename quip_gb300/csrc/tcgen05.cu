@@ -236,6 +236,44 @@ __device__ __forceinline__ void epilogue_chunk(const EpiParams& ep, int row, int
     }
 }
 
+// TF32 epilogue of one 32 x 32 block of a warp (row row0 + lane in this thread) through
+// its 4 KB shared-memory stage: each thread writes its row (16-byte chunks XOR-swizzled
+// by the row, conflict-free), then every store instruction writes 4 rows x 128
+// contiguous bytes instead of 32 scattered 16-byte pieces.
+template <int EPI>
+__device__ __forceinline__ void epilogue_chunk_staged(const EpiParams& ep, int row0, int lane, int col0, const float* v,
+                                                      float& e_acc, float* stg) {
+    float w[32];
+    if constexpr (EPI == EPI_KERNEL) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float k = v[j], cf = ep.coef[col0 + j];
+            float km1;
+            if (ep.izeta == 4) km1 = k * k * k;
+            else if (ep.izeta > 0) { km1 = 1.f; for (int t = 1; t < ep.izeta; ++t) km1 *= k; }
+            else km1 = powf(k, ep.zeta - 1.f);
+            e_acc += cf * km1 * k;
+            w[j] = round_tf32(cf * ep.zeta * km1);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) w[j] = v[j];
+    }
+    float4* srow = reinterpret_cast<float4*>(stg + lane * 32);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) srow[c ^ (lane & 7)] = make_float4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+    __syncwarp();
+    float* out = reinterpret_cast<float*>(ep.out_hi);
+    const int c = lane & 7;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int r = 4 * i + (lane >> 3);
+        const float4 val = reinterpret_cast<const float4*>(stg + r * 32)[c ^ (r & 7)];
+        if (row0 + r < ep.rows) __stcs(reinterpret_cast<float4*>(out + (size_t)(row0 + r) * ep.ldo + col0) + c, val);
+    }
+    __syncwarp();  // the stage is rewritten by the next block
+}
+
 // C[m, n] = sum_k A[m, k] B[n, k] over m_tiles x n_tiles output tiles of BM x BN.
 template <int MODE, int EPI, int BN>
 __global__ void __launch_bounds__(THREADS, 1)
@@ -439,6 +477,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     constexpr int S = C::STAGES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    float* epi_stage = reinterpret_cast<float*>(smem + (size_t)S * C::STAGE);  // 4 epilogue warps x 4 KB
     __shared__ __align__(8) uint64_t full[S], empty[S], tfull[2], tempty[2], drain;
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
@@ -534,7 +573,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int cc = 0; cc < width / 32; ++cc) {
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_STRIDE + cc * 32, v);
-                if (row < ep.rows) epilogue_chunk<MODE_TF32, EPI>(ep, row, n0 + cc * 32, v, e_acc);
+                epilogue_chunk_staged<EPI>(ep, m0 + q * 32, lane, n0 + cc * 32, v, e_acc, epi_stage + q * 1024);
                 if constexpr (EPI == EPI_KERNEL) {
                     if (cc & 1) {
                         if (row < ep.rows) ep.epart[(size_t)row * ep.ntiles + (n0 + cc * 32) / 64] = (double)e_acc;
@@ -689,7 +728,7 @@ template <int EPI, int BN>
 int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, int rows, int N, int kchunks, EpiParams ep,
                 int* err) {
     using Cf = PairCfg<BN>;
-    const int smem = Cf::STAGES * Cf::STAGE + 1024;
+    const int smem = Cf::STAGES * Cf::STAGE + 4 * 4096 + 1024;  // stage ring, epilogue stages, alignment
     GG_CUDA(cudaFuncSetAttribute(k_tc_gemm_pair<EPI, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     const int m_tiles = (rows + 2 * BM - 1) / (2 * BM), n_tiles = (N + BN - 1) / BN;
     if (EPI == EPI_KERNEL) ep.ntiles = N / 64;  // energy blocks of 64 columns
