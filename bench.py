@@ -243,6 +243,8 @@ def main():
     ap.add_argument("--serving-seconds", type=float, default=3.0)
     ap.add_argument("--gemm-pairs", type=int, default=1, choices=[0, 1, 2],
                     help="CTA-pair GEMM tiles: 0 off, 1 autotuner candidates, 2 only")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="GEMM tiles by the built-in rule instead of timing the candidates (profiling)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -324,6 +326,8 @@ def main():
 
     pot = Potential(param_filename=path, precision=args.precision)
     pot.set_option("pairs", args.gemm_pairs)
+    if args.no_autotune:
+        pot.set_option("autotune", 0)
     clk = Clocks(os.path.join(tmp, "clocks.csv"))
     with clk:
         t_wall0 = time.perf_counter()

@@ -843,7 +843,9 @@ int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune[key] = te;
     }
-    if (!BN) BN = pairs == 2 ? (N >= 256 ? -256 : -128) : pick_bn(MODE, N);
+    // without a timing (inside a capture, or autotuning off): 256-wide pair tiles where
+    // enabled -- the fastest candidate at every row count measured on GB300
+    if (!BN) BN = pairs >= 1 ? (N >= 256 ? -256 : -128) : pick_bn(MODE, N);
     CUtensorMap a0, a1, b0, b1;
     if ((rc = maps(BN, a0, a1, b0, b1))) return rc;
     if (ntiles_out) *ntiles_out = N / 64;
