@@ -422,15 +422,16 @@ def main():
         mult = 3.0
         peak = pk["bf16_tflops"] / mult
         bound, pnote = "tensor", "of measured: bf16 burst %.1f TF/s / 3 (3 split-BF16 products)" % pk["bf16_tflops"]
-    # DRAM bytes of the two GEMM launches from the committed ncu capture of the 8192-atom
-    # case with this model (profiles/ncu_full_sic8192_tf32.md: 746+248 and 623+56 MB),
-    # scaled by the row count: the operand re-reads and the W/G writes grow with the rows
+    # DRAM bytes of the two GEMM launches from the ncu capture of the 8192-atom case with
+    # this model (CTA-pair tiles: 712+240 MB and 589+44 MB read+written), scaled by the row
+    # count: the operand re-reads and the W/G writes grow with the rows
     traffic = None
     if args.precision == "tf32" and w["kind"] == "sic":
-        traffic = (746 + 248 + 623 + 56) * 1e6 * n / 8192
+        traffic = (712 + 240 + 589 + 44) * 1e6 * n / 8192
     kernel = ("sparse-GP kernel GEMMs (FP64 SIMT k_gemm_nt_epi: K = Q X^T with fused kernel epilogue, k_gemm_nn: "
               "G = W X)" if args.precision == "fp64" else
-              "sparse-GP kernel GEMMs (k_tc_gemm x2: K = Q X^T with fused kernel epilogue, G = W X)")
+              "sparse-GP kernel GEMMs (tcgen05, tiles chosen by the autotuner -- k_tc_gemm_pair on CTA pairs at "
+              "this size: K = Q X^T with fused kernel epilogue, G = W X)")
     roofline = {"bound": bound, "kernel": kernel,
                 "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s",
                 "frac": (gemm_tflops / peak) if gemm_tflops else None, "traffic": traffic,
