@@ -56,6 +56,10 @@ struct SoapConst {
     double T[MAX_NMAX * MAX_NMAX];
     double centre_R[MAX_NMAX];
     int centre_all;
+    // Per-warp task lists of the forward kernel's neighbour-function phase (lane =
+    // neighbour), longest first to the least-loaded of the 8 warps.  Task id a < n_max:
+    // radial row a; n_max + m: Ylm column m; 0xff ends a list.
+    unsigned char fsched[8][8];
 };
 
 struct Coordinate {

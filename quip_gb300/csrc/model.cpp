@@ -258,6 +258,32 @@ void soap_setup(SoapParams& s) {
     }
 }
 
+// Longest-processing-time assignment of the forward kernel's neighbour-function tasks to
+// its 8 warps (the costs are relative step counts of the recurrences).
+static void schedule_functions(const SoapParams& s, SoapConst& k) {
+    const int L = s.l_max + 1, nm = s.n_max;
+    struct Task { double cost; int code; };
+    auto radial = [&](int a) { return s.rb[a] == 0.0 ? 2.0 : 4.0 + L; };
+    auto ylm = [&](int m) { return 1.0 + 0.5 * m + 1.2 * (L - m); };
+    auto assign = [](std::vector<Task> tasks, auto put) {
+        std::stable_sort(tasks.begin(), tasks.end(), [](const Task& x, const Task& y) { return x.cost > y.cost; });
+        double load[8] = {0};
+        int used[8] = {0};
+        for (const Task& t : tasks) {
+            int w = -1;
+            for (int i = 0; i < 8; ++i)
+                if (used[i] < 8 && (w < 0 || load[i] < load[w])) w = i;
+            put(w, used[w]++, t.code);
+            load[w] += t.cost;
+        }
+    };
+    std::memset(k.fsched, 0xff, sizeof k.fsched);
+    std::vector<Task> f;
+    for (int a = 0; a < nm; ++a) f.push_back({radial(a), a});
+    for (int m = 0; m < L; ++m) f.push_back({ylm(m), nm + m});
+    assign(f, [&](int w, int j, int code) { k.fsched[w][j] = (unsigned char)code; });
+}
+
 SoapConst soap_const(const Coordinate& c) {
     SoapConst k;
     std::memset(&k, 0, sizeof k);
@@ -271,6 +297,7 @@ SoapConst soap_const(const Coordinate& c) {
     for (int i = 0; i < s.n_max; ++i) { k.rb[i] = s.rb[i]; k.centre_R[i] = s.centre_R[i]; }
     for (int i = 0; i < s.n_max * s.n_max; ++i) k.T[i] = s.T[i];
     k.centre_all = s.central_all;
+    schedule_functions(s, k);
     return k;
 }
 

@@ -233,6 +233,7 @@ __device__ __forceinline__ int l_of_lm(int lm) {
 constexpr int FWD_THREADS = 256;
 constexpr int TC = 32;   // neighbours staged per chunk in the forward kernel
 constexpr int TCB = 16;  // ... and in the backward kernel (dual Ylm staging is 4x larger)
+static_assert(TC == 32 && TCB == 16, "the neighbour-function phases map lanes to staged neighbours");
 
 // Neighbour data of one chunk, loaded into registers one chunk ahead of its staging so
 // that the dependent loads (list -> atomic number) overlap the previous chunk's work:
@@ -508,21 +509,23 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
             }
         }
         __syncthreads();
-        // Ylm columns and radial rows of the staged neighbours as one task list: first the
-        // columns, m descending with the neighbour fastest (a warp's lanes share m, so the
-        // recurrences run equally long), then the rows (t, a) of the n_max basis functions
-        const int nY = cnt * L, nT = nY + cnt * nm;
-        for (int k = tid; k < nT; k += bd) {
-            if (k < nY) {
-                const int mi = k / cnt, t = k - mi * cnt;
-                if (spc[t] < 0) continue;
+        // Ylm columns and radial rows of the staged neighbours: lane = neighbour, each warp
+        // runs its task list (warp-uniform branches, no per-task index decoding)
+        {
+            const int t = tid & 31, wid = tid >> 5;
+            const bool act = t < cnt && spc[t] >= 0;
+            R ux = 0, uy = 0, uz = 1, r = 1, fc = 0;
+            if (act) {
                 const R* u = dsm + DS * t;
-                ylm_column<R>(L - 1 - mi, L, u[0], u[1], u[2], K, tb, Ysm + t * L2);
-            } else {
-                const int k2 = k - nY, t = k2 / nm, a = k2 - t * nm;
-                if (spc[t] < 0) continue;
-                radial_collocation<R>(dsm[DS * t + 4], K[tb.rb + a], alpha, L, fcs[t], Ism + t * L * NMP + a,
-                                      (R*)nullptr, NMP);
+                ux = u[0]; uy = u[1]; uz = u[2]; r = u[4]; fc = fcs[t];
+            }
+#pragma unroll 1
+            for (int j = 0; j < 8; ++j) {
+                const int task = sc.fsched[wid][j];
+                if (task == 0xff) break;
+                if (!act) continue;
+                if (task < nm) radial_collocation<R>(r, K[tb.rb + task], alpha, L, fc, Ism + t * L * NMP + task, (R*)nullptr, NMP);
+                else ylm_column<R>(task - nm, L, ux, uy, uz, K, tb, Ysm + t * L2);
             }
         }
         __syncthreads();
@@ -634,6 +637,7 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
 }
 
 constexpr int BWD_THREADS = 256;
+static_assert(FWD_THREADS == 256 && BWD_THREADS == 256, "8 warps: the rows of the task schedules");
 constexpr int BWD_WARPS = BWD_THREADS / 32;
 
 // Shared-memory plan of the backward kernel (elements of R): constant block, h, then a
@@ -816,8 +820,9 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
         prev_cnt = cnt;
         __syncthreads();
         if (base + TCB < p1) nf.load<TCB>(base + TCB, p1, Z, nj, nd);
-        // one task list as in the forward kernel: Ylm columns (m descending, neighbour
-        // fastest), then the radial rows (t, a) with their r-derivatives
+        // one task list: Ylm columns (m descending, neighbour fastest, so a warp's lanes
+        // share m and the recurrences run equally long), then the radial rows (t, a) with
+        // their r-derivatives
         const int nY = cnt * L, nT = nY + cnt * nm;
         for (int k = tid; k < nT; k += bd) {
             if (k < nY) {
