@@ -118,7 +118,10 @@ int gapgpu_calc_batch(gapgpu_context* ctx, int nstruct, const int32_t* n_atoms, 
  * call); "timing" (0/1): per-stage CUDA events (gapgpu_context_timings); "priority"
  * (0/1): run on a stream of default or highest scheduling priority (latency-critical
  * requests next to background MD); "autotune" (0/1, default 1): time the tensor-core
- * GEMM's tile candidates on the first GEMM of each new shape and keep the fastest. */
+ * GEMM's tile candidates on the first GEMM of each new shape and keep the fastest;
+ * "pairs" (0/1/2, default 1, TF32 only): GEMM tiles on CTA pairs (256-row tiles computed
+ * by two SMs, tcgen05 cta_group::2) -- 0 never, 1 as autotuner candidates next to the
+ * single-CTA tiles (and the choice when no timing is possible), 2 only. */
 int gapgpu_context_set_option(gapgpu_context* ctx, const char* key, int value);
 
 /* Text report of the autotuner's choices so far (one line per GEMM shape: chosen N tile

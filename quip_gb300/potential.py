@@ -157,7 +157,8 @@ class Potential:
         return out
 
     def set_option(self, key, value):
-        """Context options: graphs (CUDA-graph replay of repeated shapes), timing."""
+        """Context options (gapgpu_context_set_option): graphs (CUDA-graph replay of
+        repeated shapes), timing, priority, autotune, pairs (CTA-pair GEMM tiles)."""
         _lib.check(self._L.gapgpu_context_set_option(self._ctx, key.encode(), int(value)))
 
     def footprint(self, n_atoms, mean_neighbours=60.0):
