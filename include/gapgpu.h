@@ -124,6 +124,15 @@ int gapgpu_calc_batch(gapgpu_context* ctx, int nstruct, const int32_t* n_atoms, 
  * single-CTA tiles (and the choice when no timing is possible), 2 only. */
 int gapgpu_context_set_option(gapgpu_context* ctx, const char* key, int value);
 
+/* energy_per_coordinate of the last gapgpu_calc / gapgpu_calc_batch whose args requested
+ * it ("energy_per_coordinate=<name>", IPModel_GAP.f95:335): per structure and coordinate
+ * (structure-major, model coordinate order) the sum of e_i * covariance_cutoff over the
+ * evaluated descriptor instances, before E_scale and without e0 (:462, :570).  *count
+ * receives nstruct * n_coordinates; GAPGPU_ERR_ARG when capacity is smaller or the last
+ * evaluation did not request the sums.  The calc argument only_descriptor=<k> (:334,
+ * :399-403) evaluates only coordinate k (1-based) of a model with more than one. */
+int gapgpu_energy_per_coordinate(gapgpu_context* ctx, double* out, int capacity, int* count);
+
 /* Text report of the autotuner's choices so far (one line per GEMM shape: chosen N tile
  * and the time of every candidate).  Returns the report length; writes at most
  * capacity-1 characters and a terminating NUL. */

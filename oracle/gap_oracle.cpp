@@ -771,8 +771,13 @@ int oracle_soap(const double* fp, const int* ip, int n, const double* pos, const
 // Full GAP calculation as IPModel_GAP_Calc (IPModel_GAP.f95:233-605).
 // Any output pointer may be NULL.  lattice column-major (columns = cell vectors),
 // force 3*n, local_virial 9*n (column-major 3x3 per atom), mask optional.
-int oracle_gap_calc(void* mp, int n, const double* pos, const int* Z, const double* lattice, const int* pbc, const int* mask,
-                    double* energy, double* local_e, double* force, double* virial, double* local_virial, int nthreads) {
+// select/only: the calc argument only_descriptor (given, 1-based value): with more than
+// one coordinate only that one is evaluated (:399-403).  epc (one value per coordinate,
+// may be NULL): energy_per_coordinate, the sum of e_i * covariance_cutoff over the
+// evaluated instances, before E_scale and without e0 (:462, :570).
+int oracle_gap_calc_ex(void* mp, int n, const double* pos, const int* Z, const double* lattice, const int* pbc,
+                       const int* mask, int select, int only, double* epc, double* energy, double* local_e, double* force,
+                       double* virial, double* local_virial, int nthreads) {
     Model& m = *static_cast<Model*>(mp);
     NeighbourList nl;
     if (build_neighbours(n, pos, lattice, pbc, model_cutoff(m), nl) != 0) return -1;
@@ -781,11 +786,16 @@ int oracle_gap_calc(void* mp, int n, const double* pos, const int* Z, const doub
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
-    for (const Coordinate& c : m.coords) {
+    const int ncoord = (int)m.coords.size();
+    if (epc) for (int k = 0; k < ncoord; ++k) epc[k] = 0.0;
+    for (int k = 0; k < ncoord; ++k) {
+        const Coordinate& c = m.coords[k];
+        if (select && ncoord > 1 && k + 1 != only) continue;
         std::vector<std::pair<int, int>> inst;
         enumerate_instances(c, n, Z, pos, nl, mask, inst);
         const long ni = (long)inst.size();
-#pragma omp parallel
+        double epc_k = 0.0;
+#pragma omp parallel reduction(+ : epc_k)
         {
             std::vector<double> le_t(n, 0.0), f_t(3 * (size_t)n, 0.0), v_t(9 * (size_t)n, 0.0);
             std::vector<double> gp(c.D);
@@ -794,6 +804,7 @@ int oracle_gap_calc(void* mp, int n, const double* pos, const int* Z, const doub
             for (long k = 0; k < ni; ++k) {
                 make_instance(c, inst[k].first, inst[k].second, Z, pos, nl, do_grad, I);
                 double e = gp_predict(c, I.x.data(), do_grad ? gp.data() : nullptr);
+                epc_k += e * I.fc;
                 double ec = e * I.fc / (double)I.ci.size();
                 for (int a : I.ci) le_t[a] += ec;
                 if (!do_grad) continue;
@@ -820,6 +831,7 @@ int oracle_gap_calc(void* mp, int n, const double* pos, const int* Z, const doub
                 for (size_t a = 0; a < vir.size(); ++a) vir[a] += v_t[a];
             }
         }
+        if (epc) epc[k] = epc_k;
     }
     double E = 0;
     for (int a = 0; a < n; ++a) E += le[a];
@@ -843,5 +855,13 @@ int oracle_gap_calc(void* mp, int n, const double* pos, const int* Z, const doub
     if (local_virial) for (size_t a = 0; a < vir.size(); ++a) local_virial[a] = s * vir[a];
     return 0;
 }
+
+int oracle_gap_calc(void* mp, int n, const double* pos, const int* Z, const double* lattice, const int* pbc, const int* mask,
+                    double* energy, double* local_e, double* force, double* virial, double* local_virial, int nthreads) {
+    return oracle_gap_calc_ex(mp, n, pos, Z, lattice, pbc, mask, 0, 0, nullptr, energy, local_e, force, virial,
+                              local_virial, nthreads);
+}
+
+int oracle_model_n_coordinates(void* mp) { return (int)static_cast<Model*>(mp)->coords.size(); }
 
 }  // extern "C"

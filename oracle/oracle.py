@@ -55,6 +55,10 @@ def lib():
         L.oracle_soap.argtypes = [P(d), P(i), i, P(d), P(i), P(d), P(i), d, P(d), l, P(d), P(i), l, P(l)]
         L.oracle_gap_calc.restype = i
         L.oracle_gap_calc.argtypes = [v, i, P(d), P(i), P(d), P(i), P(i), P(d), P(d), P(d), P(d), P(d), i]
+        L.oracle_gap_calc_ex.restype = i
+        L.oracle_gap_calc_ex.argtypes = [v, i, P(d), P(i), P(d), P(i), P(i), i, i, P(d), P(d), P(d), P(d), P(d), P(d), i]
+        L.oracle_model_n_coordinates.restype = i
+        L.oracle_model_n_coordinates.argtypes = [v]
         _lib = L
     return _lib
 
@@ -245,8 +249,11 @@ class OracleModel:
         except Exception:
             pass
 
-    def calc(self, pos, Z, lattice, pbc=(1, 1, 1), mask=None, nthreads=0):
-        """E, local_e, F (N,3), virial (3,3), local_virial (N,3,3)."""
+    def calc(self, pos, Z, lattice, pbc=(1, 1, 1), mask=None, nthreads=0, only_descriptor=None):
+        """E, local_e, F (N,3), virial (3,3), local_virial (N,3,3) and energy_per_coordinate
+        (one value per coordinate: sum of e_i * covariance_cutoff, before E_scale, no e0).
+        only_descriptor: the calc argument of that name (1-based coordinate; with more than
+        one coordinate only that one is evaluated)."""
         pos = np.ascontiguousarray(pos, dtype=np.float64)
         n = len(pos)
         Z = np.ascontiguousarray(Z, dtype=np.int32)
@@ -254,9 +261,12 @@ class OracleModel:
         pbc = np.ascontiguousarray(np.asarray(pbc, dtype=np.int32).reshape(3))
         m = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
         E = np.zeros(1); le = np.zeros(n); F = np.zeros((n, 3)); V = np.zeros(9); LV = np.zeros((n, 9))
-        rc = lib().oracle_gap_calc(self._h, n, _dp(pos), _ip(Z), _dp(lat), _ip(pbc), _ip(m), _dp(E), _dp(le), _dp(F),
-                                   _dp(V), _dp(LV), nthreads)
+        epc = np.zeros(lib().oracle_model_n_coordinates(self._h))
+        sel = only_descriptor is not None
+        rc = lib().oracle_gap_calc_ex(self._h, n, _dp(pos), _ip(Z), _dp(lat), _ip(pbc), _ip(m), int(sel),
+                                      int(only_descriptor) if sel else 0, _dp(epc), _dp(E), _dp(le), _dp(F), _dp(V),
+                                      _dp(LV), nthreads)
         if rc != 0:
             raise RuntimeError("oracle_gap_calc failed")
         return dict(energy=E[0], local_energy=le, force=F, virial=V.reshape(3, 3, order="F"),
-                    local_virial=LV.reshape(n, 3, 3).transpose(0, 2, 1))
+                    local_virial=LV.reshape(n, 3, 3).transpose(0, 2, 1), energy_per_coordinate=epc)

@@ -21,7 +21,7 @@ EXPORTS = ["gapgpu_last_error", "gapgpu_model_create", "gapgpu_model_cutoff", "g
            "gapgpu_context_timings", "gapgpu_context_launches", "gapgpu_neighbours_static", "gapgpu_calc_batch",
            "gapgpu_context_set_option", "gapgpu_model_footprint", "gapgpu_md_create", "gapgpu_md_step", "gapgpu_md_state",
            "gapgpu_md_counters", "gapgpu_md_context", "gapgpu_md_destroy", "gapgpu_tuning_report",
-           "gapgpu_selftest_bounded_wait", "gapgpu_calc_lammps"]
+           "gapgpu_selftest_bounded_wait", "gapgpu_calc_lammps", "gapgpu_energy_per_coordinate"]
 
 
 class GapGpuError(RuntimeError):
@@ -86,6 +86,7 @@ def load(build_if_missing=True):
                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
     L.gapgpu_context_timings.argtypes = [c_void_p, P(c_double), c_int]
     L.gapgpu_context_launches.argtypes = [c_void_p, P(i64)]
+    L.gapgpu_energy_per_coordinate.argtypes = [c_void_p, c_void_p, c_int, P(c_int)]
     _lib = L
     return L
 

@@ -24,6 +24,8 @@ size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
 struct ArgOpts {
     int precision = -1;
     bool bad_scale = false;
+    bool select = false, epc = false;  // only_descriptor given; energy_per_coordinate requested
+    int only = 0;
 };
 
 int parse_calc_args(const char* args, ArgOpts& o) {
@@ -41,12 +43,32 @@ int parse_calc_args(const char* args, ArgOpts& o) {
         else if (p == "tf32") o.precision = GAPGPU_MIXED_TF32;
         else GG_FAIL(GAPGPU_ERR_ARG, "precision must be fp64, bf16x3 or tf32");
     }
-    for (const char* k : {"local_gap_variance", "print_gap_variance", "energy_per_coordinate", "only_descriptor"}) {
+    for (const char* k : {"local_gap_variance", "print_gap_variance"}) {
         auto it = a.find(k);
         if (it != a.end() && it->second != "" && it->second != "F" && it->second != "0")
             GG_FAIL(GAPGPU_ERR_UNSUPPORTED, std::string("calc option ") + k + " is not supported by this library");
     }
+    // only_descriptor (IPModel_GAP.f95:334, :399-403): given at all, it selects the coordinate
+    // of that 1-based index when the model has more than one
+    auto od = a.find("only_descriptor");
+    if (od != a.end()) {
+        char* end = nullptr;
+        const long v = std::strtol(od->second.c_str(), &end, 10);
+        if (od->second.empty() || *end) GG_FAIL(GAPGPU_ERR_ARG, "only_descriptor must be an integer");
+        o.select = true;
+        o.only = (int)v;
+    }
+    // energy_per_coordinate=name (:335, :462, :570): a non-empty name requests the sums
+    auto ep = a.find("energy_per_coordinate");
+    o.epc = ep != a.end() && !ep->second.empty();
     return GAPGPU_OK;
+}
+
+void apply_call_opts(gapgpu_context& c, const ArgOpts& o) {
+    c.sel_coord = o.select;
+    c.only_coord = o.only;
+    c.want_epc = o.epc;
+    c.epc_valid = false;
 }
 
 int check_device() {
@@ -62,6 +84,12 @@ int check_device() {
 }
 
 }  // namespace
+
+// only_descriptor selects coordinate k (0-based) only when the model has more than one
+// (IPModel_GAP.f95:399-403)
+bool coordinate_chosen(const gapgpu_context& c, int k) {
+    return !c.sel_coord || c.model->coords.size() <= 1 || k + 1 == c.only_coord;
+}
 
 int upload_model(gapgpu_model& m) {
     int rc;
@@ -204,14 +232,24 @@ int evaluate(gapgpu_context& c, int precision, const int* d_mask, bool timed) {
         GG_CUDA(cudaMemsetAsync(c.eatom.p, 0, sizeof(double) * n, c.stream));
         const int saved = c.precision;
         c.precision = precision;
+        const int ncoord = (int)m.coords.size();
+        if (c.want_epc) {
+            if ((rc = c.epc_out.ensure(sizeof(double) * (size_t)ncoord * c.nstruct))) return rc;
+            GG_CUDA(cudaMemsetAsync(c.epc_out.p, 0, sizeof(double) * (size_t)ncoord * c.nstruct, c.stream));
+        }
         // the distance_2b coordinates run together, in one pass over the pairs, at the
         // position of the first of them
         std::vector<const Coordinate*> two_body;
-        for (const Coordinate& co : m.coords)
-            if (co.type != DESC_SOAP) two_body.push_back(&co);
+        std::vector<int> two_body_k;
+        for (int k = 0; k < ncoord; ++k)
+            if (m.coords[k].type != DESC_SOAP && coordinate_chosen(c, k)) {
+                two_body.push_back(&m.coords[k]);
+                two_body_k.push_back(k);
+            }
         bool two_body_done = false;
-        for (int k = 0; k < (int)m.coords.size() && !rc; ++k) {
+        for (int k = 0; k < ncoord && !rc; ++k) {
             const Coordinate& co = m.coords[k];
+            if (!coordinate_chosen(c, k)) continue;
             if (co.type == DESC_SOAP) {
                 const int nc = c.nc_coord[k];
                 c.cur_centres = c.centres.as<int>() + (size_t)k * n;
@@ -219,6 +257,7 @@ int evaluate(gapgpu_context& c, int precision, const int* d_mask, bool timed) {
                 if ((rc = soap_forward(c, co, n, nc))) break;
                 record(c, timed);
                 rc = precision == GAPGPU_FP64 ? gp_fp64(c, co, nc) : gp_mixed(c, co, nc, precision);
+                if (!rc && c.want_epc) rc = epc_soap(c, k, nc, n);
                 if (rc) break;
                 record(c, timed);
                 if ((rc = soap_backward(c, co, n, nc))) break;
@@ -226,6 +265,8 @@ int evaluate(gapgpu_context& c, int precision, const int* d_mask, bool timed) {
                 two_body_done = true;
                 record(c, timed);
                 if ((rc = pair_2b(c, two_body, d_mask))) break;
+                for (size_t j = 0; j < two_body.size() && c.want_epc && !rc; ++j)
+                    rc = epc_pair(c, *two_body[j], two_body_k[j], d_mask);
             }
         }
         c.precision = saved;
@@ -243,7 +284,8 @@ int evaluate(gapgpu_context& c, int precision, const int* d_mask, bool timed) {
 std::vector<uintptr_t> graph_key(const gapgpu_context& c, int precision, const int* d_mask) {
     std::vector<uintptr_t> k = {(uintptr_t)precision, (uintptr_t)d_mask, (uintptr_t)c.n_total, (uintptr_t)c.nstruct,
                                 (uintptr_t)c.n_pairs, (uintptr_t)c.model, (uintptr_t)c.stream,
-                                (uintptr_t)c.h_chunks.size()};
+                                (uintptr_t)c.h_chunks.size(), (uintptr_t)c.sel_coord, (uintptr_t)(intptr_t)c.only_coord,
+                                (uintptr_t)c.want_epc};
     for (int nc : c.nc_coord) k.push_back((uintptr_t)nc);
     for (const gapgpu::DBuf* b : c.buffers()) k.push_back((uintptr_t)b->p);
     return k;
@@ -339,7 +381,9 @@ void compute_timings(gapgpu_context& c) {
         int i = 1;
         bool two_body_done = false;
         t.reduce += el(c.cev[0], c.cev[1]);  // output zeroing
-        for (const Coordinate& co : c.model->coords) {
+        for (int kc = 0; kc < (int)c.model->coords.size(); ++kc) {
+            const Coordinate& co = c.model->coords[kc];
+            if (!coordinate_chosen(c, kc)) continue;
             if (co.type == DESC_SOAP) {
                 if (i + 3 >= c.ncev) break;
                 t.soap_fwd += el(c.cev[i], c.cev[i + 1]);
@@ -466,6 +510,18 @@ int gapgpu_context_set_stream(gapgpu_context* c, void* s) {
     return GAPGPU_OK;
 }
 
+int gapgpu_energy_per_coordinate(gapgpu_context* c, double* out, int capacity, int* count) {
+    if (!c || !out || !count) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_energy_per_coordinate: NULL argument");
+    if (!c->epc_valid)
+        GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_energy_per_coordinate: the last evaluation did not request energy_per_coordinate");
+    const int n = c->nstruct * (int)c->model->coords.size();
+    *count = n;
+    if (capacity < n) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_energy_per_coordinate: output too small");
+    GG_CUDA(cudaMemcpyAsync(out, c->epc_out.p, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    GG_CUDA(cudaStreamSynchronize(c->stream));
+    return GAPGPU_OK;
+}
+
 int gapgpu_context_set_option(gapgpu_context* c, const char* key, int value) {
     if (!c || !key) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_set_option: NULL argument");
     const std::string k(key);
@@ -508,6 +564,7 @@ int gapgpu_calc(gapgpu_context* c, int n, const double* pos, const int32_t* Z, c
     ArgOpts o;
     int rc;
     if ((rc = parse_calc_args(args, o))) return rc;
+    apply_call_opts(*c, o);
     const int prec = o.precision >= 0 ? o.precision : c->precision;
     if (n == 0) {
         if (energy) *energy = 0;
@@ -518,6 +575,7 @@ int gapgpu_calc(gapgpu_context* c, int n, const double* pos, const int32_t* Z, c
     const int* dmask = atom_mask ? c->mask.as<int>() : nullptr;
     if ((rc = prepare(*c, 1, &n, lattice, pbc, dmask, c->model->cutoff, LIST_BUILD, prec))) return rc;
     if ((rc = run_evaluation(*c, prec, dmask))) return rc;
+    c->epc_valid = c->want_epc;
     double red[10];
     GG_CUDA(cudaMemcpyAsync(red, c->out_e.p, sizeof red, cudaMemcpyDeviceToHost, c->stream));
     if (force) GG_CUDA(cudaMemcpyAsync(force, c->out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
@@ -538,6 +596,7 @@ int gapgpu_calc_device(gapgpu_context* c, int n, const double* d_pos, const int3
     int rc;
     if ((rc = copy_inputs(*c, n, d_pos, d_Z, nullptr, cudaMemcpyDeviceToDevice))) return rc;
     if ((rc = prepare(*c, 1, &n, lattice, pbc, nullptr, c->model->cutoff, LIST_BUILD, c->precision))) return rc;
+    apply_call_opts(*c, ArgOpts{});
     if ((rc = run_evaluation(*c, c->precision, nullptr))) return rc;
     if (d_energy) GG_CUDA(cudaMemcpyAsync(d_energy, c->out_e.p, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     if (d_virial)
@@ -554,6 +613,7 @@ int gapgpu_calc_batch(gapgpu_context* c, int nstruct, const int32_t* n_atoms, co
     ArgOpts o;
     int rc;
     if ((rc = parse_calc_args(args, o))) return rc;
+    apply_call_opts(*c, o);
     const int prec = o.precision >= 0 ? o.precision : c->precision;
     long long n = 0;
     for (int s = 0; s < nstruct; ++s) {
@@ -565,6 +625,7 @@ int gapgpu_calc_batch(gapgpu_context* c, int nstruct, const int32_t* n_atoms, co
     if ((rc = copy_inputs(*c, (int)n, pos, Z, nullptr, cudaMemcpyHostToDevice))) return rc;
     if ((rc = prepare(*c, nstruct, n_atoms, lattices, pbcs, nullptr, c->model->cutoff, LIST_BUILD, prec))) return rc;
     if ((rc = run_evaluation(*c, prec, nullptr))) return rc;
+    c->epc_valid = c->want_epc;
     std::vector<double> red(10 * (size_t)nstruct);
     GG_CUDA(cudaMemcpyAsync(red.data(), c->out_e.p, sizeof(double) * red.size(), cudaMemcpyDeviceToHost, c->stream));
     if (forces && n > 0)
@@ -627,7 +688,9 @@ int gapgpu_calc_lammps(gapgpu_context* c, int nlocal, int nghost, const int32_t*
     if ((rc = load_external_neighbours(*c, n, off, nj, lattice, prec != GAPGPU_FP64))) return rc;
     const int pbc[3] = {0, 0, 0};
     if ((rc = prepare(*c, 1, &n, lattice, pbc, dmask, c->model->cutoff, LIST_GIVEN, prec))) return rc;
+    apply_call_opts(*c, ArgOpts{});
     if ((rc = run_evaluation(*c, prec, dmask))) return rc;
+    c->epc_valid = c->want_epc;
     double red[10];
     GG_CUDA(cudaMemcpyAsync(red, c->out_e.p, sizeof red, cudaMemcpyDeviceToHost, c->stream));
     if (force) GG_CUDA(cudaMemcpyAsync(force, c->out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));

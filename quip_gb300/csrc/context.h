@@ -70,6 +70,11 @@ struct gapgpu_context {
     int* cur_centres = nullptr;               // centre list of the coordinate being evaluated
     std::vector<int> nc_coord;                // centres per coordinate (prepare phase)
     gapgpu::DBuf chunks, schunk;              // segmented-reduction tables (per batch)
+    // calc arguments of the current evaluation (IPModel_GAP.f95:334-335): only_descriptor
+    // (given, 1-based value) and energy_per_coordinate
+    bool sel_coord = false, want_epc = false, epc_valid = false;
+    int only_coord = 0;
+    gapgpu::DBuf epc_out, epca, epcp;         // [nstruct x ncoord]; per-atom and per-pair scratch
     std::vector<int> h_chunks, h_schunk;
     int nstruct = 0, n_total = 0;
     // CUDA graph of the evaluation phase, keyed by shapes and buffer addresses
@@ -92,7 +97,8 @@ struct gapgpu_context {
         return {&pos, &Z, &mask, &out_e, &out_f, &out_le, &out_lv, &cell_key, &cell_key2, &atom_idx, &atom_idx2,
                 &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev,
                 &nbr_i, &wpos, &total, &geoms, &sid, &dispmax, &phi, &plo, &fpair, &epair, &eatom, &redpart, &flags, &centres,
-                &ncent, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf, &Wlo, &epart, &ecent, &Gbuf, &scratch, &chunks, &schunk};
+                &ncent, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf, &Wlo, &epart, &ecent, &Gbuf, &scratch, &chunks, &schunk,
+                &epc_out, &epca, &epcp};
     }
     std::vector<const gapgpu::DBuf*> buffers() const {
         std::vector<gapgpu::DBuf*> b = const_cast<gapgpu_context*>(this)->buffers();
@@ -126,5 +132,11 @@ int gp_fp64(gapgpu_context& c, const Coordinate& co, int nc);
 int gp_mixed(gapgpu_context& c, const Coordinate& co, int nc, int precision);
 // pair.cu
 int pair_2b(gapgpu_context& c, const std::vector<const Coordinate*>& coords, const int* d_mask);
+// energy_per_coordinate: coordinate k's sum of e_i * covariance_cutoff per structure into
+// epc_out[s * ncoord + k] -- SOAP from the per-centre energies in ecent, distance_2b from
+// one pass over the pairs
+int epc_soap(gapgpu_context& c, int k, int nc, int n);
+int epc_pair(gapgpu_context& c, const Coordinate& co, int k, const int* d_mask);
+bool coordinate_chosen(const gapgpu_context& c, int k);
 int gather_outputs(gapgpu_context& c, const gapgpu_model& m, int n, const int* d_mask);
 }  // namespace gapgpu

@@ -192,7 +192,115 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_final(const int* __restr
     if (threadIdx.x < 10) out[10 * (size_t)blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
 }
 
+// energy_per_coordinate of one distance_2b coordinate: per canonical pair, e fc times the
+// number of its two directed instances whose centre is evaluated (instance i -> j is in
+// the sum when atom i is in the mask); 0 in every other pair slot.
+template <class R>
+__global__ void k_pair_2b_energy(long long P, const int* __restrict__ Z, const int* __restrict__ mask,
+                                 const int* __restrict__ ni, const int* __restrict__ nj, const int* __restrict__ ns,
+                                 const double4* __restrict__ nd, const Pair2bSet::Entry cd, double* __restrict__ out) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    double v = 0.0;
+    const int a = ni[p], b = nj[p];
+    bool canonical = a < b;
+    if (a == b) {
+        int s = ns[p];
+        int s0 = (s & 1023) - 512, s1 = ((s >> 10) & 1023) - 512, s2 = ((s >> 20) & 1023) - 512;
+        canonical = s0 > 0 || (s0 == 0 && (s1 > 0 || (s1 == 0 && s2 > 0)));
+    }
+    const double4 d = nd[p];
+    if (canonical && d.w < cd.rc) {
+        const int za = Z[a], zb = Z[b];
+        const bool zi1 = cd.Z1 == 0 || za == cd.Z1, zj2 = cd.Z2 == 0 || zb == cd.Z2;
+        const bool zi2 = cd.Z2 == 0 || za == cd.Z2, zj1 = cd.Z1 == 0 || zb == cd.Z1;
+        const int w = (!mask || mask[a] ? 1 : 0) + (!mask || mask[b] ? 1 : 0);
+        if (((zi1 && zj2) || (zi2 && zj1)) && w > 0) {
+            const R* X = static_cast<const R*>(cd.X);
+            const R* coef = static_cast<const R*>(cd.coef);
+            const R r = (R)d.w, it2 = (R)cd.it2;
+            R e = 0;
+            for (int s = 0; s < cd.M; ++s) {
+                const R t = r - X[s];
+                e += coef[s] * exp(-(R)0.5 * t * t * it2);
+            }
+            R f, df;
+            fcut<R>(r, (R)cd.rc, (R)cd.w, f, df);
+            v = (double)w * (double)(e * f);
+        }
+    }
+    out[p] = v;
+}
+
+__global__ void k_scatter_centres(int nc, const int* __restrict__ centres, const double* __restrict__ ecent,
+                                  double* __restrict__ ea) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nc) ea[centres[i]] = ecent[i];
+}
+
+// One block per structure: the sum of vals over the structure's atoms (off == NULL) or its
+// pair slots (the CSR rows of its atoms), in a fixed order -> out[s * ncoord + k].
+__global__ void __launch_bounds__(RED_THREADS) k_epc_reduce(const double* __restrict__ vals,
+                                                           const GeomDev* __restrict__ geoms, const int* __restrict__ off,
+                                                           int ncoord, int k, double* __restrict__ out) {
+    __shared__ double sh[RED_THREADS];
+    const GeomDev& g = geoms[blockIdx.x];
+    const long long b = off ? off[g.atom_begin] : g.atom_begin, e = off ? off[g.atom_end] : g.atom_end;
+    double acc = 0.0;
+    for (long long i = b + threadIdx.x; i < e; i += RED_THREADS) acc += vals[i];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int st = RED_THREADS / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[(size_t)blockIdx.x * ncoord + k] = sh[0];
+}
+
 }  // namespace
+
+int epc_soap(gapgpu_context& c, int k, int nc, int n) {
+    int rc;
+    if ((rc = c.epca.ensure(sizeof(double) * (size_t)std::max(n, 1)))) return rc;
+    GG_CUDA(cudaMemsetAsync(c.epca.p, 0, sizeof(double) * (size_t)n, c.stream));
+    if (nc > 0)
+        k_scatter_centres<<<(nc + 127) / 128, 128, 0, c.stream>>>(nc, c.cur_centres, c.ecent.as<double>(),
+                                                                 c.epca.as<double>());
+    k_epc_reduce<<<c.nstruct, RED_THREADS, 0, c.stream>>>(c.epca.as<double>(), c.geoms.as<GeomDev>(), nullptr,
+                                                         (int)c.model->coords.size(), k, c.epc_out.as<double>());
+    c.launches += nc > 0 ? 2 : 1;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
+int epc_pair(gapgpu_context& c, const Coordinate& co, int k, const int* d_mask) {
+    const long long P = c.n_pairs;
+    if (P == 0) return GAPGPU_OK;  // no pairs: the zeroed output stands
+    int rc;
+    if ((rc = c.epcp.ensure(sizeof(double) * (size_t)P))) return rc;
+    const bool fp64 = c.precision == GAPGPU_FP64;
+    {
+        Pair2bSet::Entry e{co.d2_rc, co.d2_w, 1.0 / (co.theta[0] * co.theta[0]), co.d2_Z1, co.d2_Z2, co.M,
+                           fp64 ? (const void*)co.dX64 : (const void*)co.dXf32,
+                           fp64 ? (const void*)co.dcoef : (const void*)co.dcoef32};
+        const int TB = 256;
+        const unsigned nb = (unsigned)((P + TB - 1) / TB);
+        if (fp64)
+            k_pair_2b_energy<double><<<nb, TB, 0, c.stream>>>(P, c.Z.as<int>(), d_mask, c.nbr_i.as<int>(),
+                                                               c.nbr_j.as<int>(), c.nbr_s.as<int>(),
+                                                               c.nbr_d.as<double4>(), e, c.epcp.as<double>());
+        else
+            k_pair_2b_energy<float><<<nb, TB, 0, c.stream>>>(P, c.Z.as<int>(), d_mask, c.nbr_i.as<int>(),
+                                                              c.nbr_j.as<int>(), c.nbr_s.as<int>(),
+                                                              c.nbr_d.as<double4>(), e, c.epcp.as<double>());
+        c.launches++;
+    }
+    k_epc_reduce<<<c.nstruct, RED_THREADS, 0, c.stream>>>(c.epcp.as<double>(), c.geoms.as<GeomDev>(), c.nbr_off.as<int>(),
+                                                         (int)c.model->coords.size(), k, c.epc_out.as<double>());
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
 
 int pair_2b(gapgpu_context& c, const std::vector<const Coordinate*>& coords, const int* d_mask) {
     for (const Coordinate* co : coords)

@@ -603,11 +603,12 @@ __global__ void k_split_q(size_t n, const float* __restrict__ q, __nv_bfloat16* 
     lo[i] = __float2bfloat16_rn(x - __bfloat162float(h));
 }
 __global__ void k_rowsum_scatter32(int nc, int ntiles, const double* __restrict__ epart, const int* __restrict__ centres,
-                                   double* __restrict__ eatom) {
+                                   double* __restrict__ ecent, double* __restrict__ eatom) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
     double s = 0;
     for (int t = 0; t < ntiles; ++t) s += epart[(size_t)i * ntiles + t];
+    if (ecent) ecent[i] = s;  // per-centre energies (energy_per_coordinate)
     eatom[centres[i]] += s;
 }
 
@@ -881,7 +882,9 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
     else
         rc = gemm<MODE, EPI_KERNEL>(c, c.qlo.p, c.qlo.p, co.dXf32, co.dXf32, nc, Mp, Dp, ep, err, &ntiles);
     if (rc) return rc;
+    if (c.want_epc && (rc = c.ecent.ensure(sizeof(double) * (size_t)nc))) return rc;
     k_rowsum_scatter32<<<(nc + 127) / 128, 128, 0, c.stream>>>(nc, ntiles, c.epart.as<double>(), c.cur_centres,
+                                                              c.want_epc ? c.ecent.as<double>() : nullptr,
                                                               c.eatom.as<double>());
     c.launches++;
     // GEMM2: G = W X, B operand = X^T rows (k = sparse index contiguous)

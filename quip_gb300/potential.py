@@ -15,6 +15,12 @@ from . import _lib
 from .atoms import Atoms
 
 
+def _epc_name(args_str):
+    """The property name of energy_per_coordinate=<name> in a calc args string, or None."""
+    m = re.search(r"(?:^|\s)energy_per_coordinate=(\S+)", args_str or "")
+    return m.group(1) if m else None
+
+
 def _init_args_from_xml(xml):
     """Default init args from the first <Potential init_args=...> tag (Potential.f95:525-538)."""
     m = re.search(r'<Potential[^>]*init_args="([^"]*)"', xml)
@@ -82,6 +88,9 @@ class Potential:
         _lib.check(self._L.gapgpu_model_info(self._model, _lib.ctypes.byref(n), dims, ns, 64))
         return [(dims[k], ns[k]) for k in range(n.value)]
 
+    def n_coordinates(self):
+        return len(self.info())
+
     def timings(self):
         ms = (_lib.ctypes.c_double * 7)()
         k = self._L.gapgpu_context_timings(self._ctx, ms, 7)
@@ -107,7 +116,9 @@ class Potential:
         """potential_calc: returns a dict with the requested quantities.
 
         energy (float), force (N,3), virial (3,3), local_energy (N,), local_virial (N,3,3).
-        ``atom_mask`` is the logical property that args_str atom_mask_name names."""
+        ``atom_mask`` is the logical property that args_str atom_mask_name names.
+        args_str "energy_per_coordinate=<name>" adds out[<name>] (one value per coordinate,
+        IPModel_GAP.f95:462,570); "only_descriptor=<k>" evaluates only coordinate k."""
         pos, Z, lat, pbc = self._arrays(at)
         n = len(pos)
         E = np.zeros(1)
@@ -130,8 +141,18 @@ class Potential:
             out["local_energy"] = LE
         if local_virial:
             out["local_virial"] = LV.reshape(n, 3, 3).transpose(0, 2, 1)
+        name = _epc_name(args_str)
+        if name:
+            out[name] = self._energy_per_coordinate(1)[0]
         self.results = out
         return out
+
+    def _energy_per_coordinate(self, nstruct):
+        ncoord = self.n_coordinates()
+        buf = np.zeros(nstruct * ncoord)
+        cnt = _lib.ctypes.c_int()
+        _lib.check(self._L.gapgpu_energy_per_coordinate(self._ctx, _lib.ptr(buf), len(buf), _lib.ctypes.byref(cnt)))
+        return buf.reshape(nstruct, ncoord)
 
     def calc_batch(self, structures, args_str=""):
         """Energies, forces and virials of many independent structures in one GPU pass
@@ -150,9 +171,13 @@ class Potential:
         V = np.zeros((len(ns), 9))
         _lib.check(self._L.gapgpu_calc_batch(self._ctx, len(ns), _lib.ptr(ns), _lib.ptr(pos), _lib.ptr(Z), _lib.ptr(lat),
                                              _lib.ptr(pbc), _lib.ptr(E), _lib.ptr(F), _lib.ptr(V), args_str.encode()))
+        name = _epc_name(args_str)
+        epc = self._energy_per_coordinate(len(ns)) if name else None
         out, a0 = [], 0
         for s, n in enumerate(ns):
             out.append({"energy": float(E[s]), "force": F[a0:a0 + n], "virial": V[s].reshape(3, 3, order="F")})
+            if name:
+                out[-1][name] = epc[s]
             a0 += n
         return out
 
