@@ -456,6 +456,16 @@ __device__ __forceinline__ void commit_pair(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar)) : "memory");
 }
 
+// Output tile t -> (row block m, column block n) in bands of `group` row blocks, the row
+// block fastest within a band: the tiles in flight at once (consecutive t over all CTAs)
+// share a few B column blocks and a few A row blocks, so both stay in L2.
+__device__ __forceinline__ void tile_mn(int t, int m_tiles, int n_tiles, int group, int& m, int& n) {
+    const int band = t / (group * n_tiles), r = t - band * group * n_tiles;
+    const int gm = min(group, m_tiles - band * group);
+    n = r / gm;
+    m = band * group + (r - n * gm);
+}
+
 template <int BN>
 struct PairCfg {
     static constexpr int TILE_A = BM * 128;        // this CTA's 128 rows of A, 32 FP32 of K
@@ -472,7 +482,7 @@ struct PairCfg {
 template <int EPI, int BN>
 __global__ void __launch_bounds__(THREADS, 1)
     k_tc_gemm_pair(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, int m_tiles, int n_tiles,
-                   int N, int kchunks, EpiParams ep, int* err) {
+                   int group, int N, int kchunks, EpiParams ep, int* err) {
     using C = PairCfg<BN>;
     constexpr int S = C::STAGES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -509,8 +519,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         int it = 0;
         bool ok = true;
         for (int tile = pair; tile < ntiles && ok; tile += npairs) {
-            const int m0 = (tile / n_tiles) * (2 * BM) + (int)rank * BM;
-            const int nb = (tile % n_tiles) * BN, width = min(BN, N - nb);
+            int mt, nt;
+            tile_mn(tile, m_tiles, n_tiles, group, mt, nt);
+            const int m0 = mt * (2 * BM) + (int)rank * BM;
+            const int nb = nt * BN, width = min(BN, N - nb);
             const int n0 = nb + (int)rank * (width / 2);
             for (int kc = 0; kc < kchunks; ++kc, ++it) {
                 const int s = it % S;
@@ -538,7 +550,9 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (t >= 2 && !mbar_wait(&tempty[buf], ((t >> 1) - 1) & 1, &abort_flag, err, 2)) break;
             fence_after();
             const uint32_t acc_addr = tmem + buf * ACC_STRIDE;
-            const uint32_t id = idesc_pair(min(BN, N - (tile % n_tiles) * BN));
+            int mt, nt;
+            tile_mn(tile, m_tiles, n_tiles, group, mt, nt);
+            const uint32_t id = idesc_pair(min(BN, N - nt * BN));
             for (int kc = 0; kc < kchunks; ++kc, ++it) {
                 const int s = it % S;
                 if (!mbar_wait(&full[s], (it / S) & 1, &abort_flag, err, 2)) { ok = false; break; }
@@ -563,7 +577,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         int t = 0;
         for (int tile = pair; tile < ntiles; tile += npairs, ++t) {
             const int buf = t & 1;
-            const int m0 = (tile / n_tiles) * (2 * BM) + (int)rank * BM, n0 = (tile % n_tiles) * BN;
+            int mt, nt;
+            tile_mn(tile, m_tiles, n_tiles, group, mt, nt);
+            const int m0 = mt * (2 * BM) + (int)rank * BM, n0 = nt * BN;
             const int width = min(BN, N - n0);
             if (!mbar_wait(&tfull[buf], (t >> 1) & 1, &abort_flag, err, 4)) break;
             fence_after();
@@ -725,6 +741,9 @@ std::vector<int> bn_candidates(int N, int pairs) {
     return c;
 }
 
+// Row blocks per band of the pair kernels' tile order.
+int pair_tile_group() { return 16; }
+
 template <int EPI, int BN>
 int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, int rows, int N, int kchunks, EpiParams ep,
                 int* err) {
@@ -751,7 +770,8 @@ int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, i
     GG_CUDA(cudaOccupancyMaxActiveClusters(&resident, k_tc_gemm_pair<EPI, BN>, &cfg));
     const int npairs = std::max(1, std::min(ntiles, resident > 0 ? resident : num_sms() / 2));
     cfg.gridDim = dim3(2 * npairs);
-    GG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_gemm_pair<EPI, BN>, a, b, m_tiles, n_tiles, N, kchunks, ep, err));
+    GG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_gemm_pair<EPI, BN>, a, b, m_tiles, n_tiles, pair_tile_group(), N, kchunks, ep,
+                               err));
     c.launches++;
     return GAPGPU_OK;
 }
