@@ -741,8 +741,11 @@ std::vector<int> bn_candidates(int N, int pairs) {
     return c;
 }
 
-// Row blocks per band of the pair kernels' tile order.
-int pair_tile_group() { return 16; }
+// Row blocks per band of the pair kernels' tile order: bands of 16 when there are many
+// column blocks (the sparse-point operand B is then the one shared by the tiles in
+// flight), none when there are few (the row blocks of A are then the large operand, and
+// the N-fastest order keeps each one in L2 until all its column blocks are done).
+int pair_tile_group(int n_tiles) { return n_tiles >= 16 ? 16 : 1; }
 
 template <int EPI, int BN>
 int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, int rows, int N, int kchunks, EpiParams ep,
@@ -770,7 +773,7 @@ int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, i
     GG_CUDA(cudaOccupancyMaxActiveClusters(&resident, k_tc_gemm_pair<EPI, BN>, &cfg));
     const int npairs = std::max(1, std::min(ntiles, resident > 0 ? resident : num_sms() / 2));
     cfg.gridDim = dim3(2 * npairs);
-    GG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_gemm_pair<EPI, BN>, a, b, m_tiles, n_tiles, pair_tile_group(), N, kchunks, ep,
+    GG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_gemm_pair<EPI, BN>, a, b, m_tiles, n_tiles, pair_tile_group(n_tiles), N, kchunks, ep,
                                err));
     c.launches++;
     return GAPGPU_OK;
