@@ -106,3 +106,26 @@ def test_oracle_forces_are_energy_gradient(golden):
         assert abs(-(e1 - e2) / (2 * h) - r["virial"][a, b]) < 1e-5
     np.testing.assert_allclose(r["local_virial"].sum(0), r["virial"], atol=1e-10)
     np.testing.assert_allclose(r["local_energy"].sum(), r["energy"], atol=1e-10)
+
+
+def test_oracle_coordinate_options(golden):
+    """only_descriptor and energy_per_coordinate (IPModel_GAP.f95:399-403, :462, :570) on the
+    water model's distance_2b coordinates: the per-coordinate energies and the isolated-atom
+    energies make up E; selecting one coordinate leaves its energy and its forces only,
+    and the selections add up to the full forces."""
+    at = _water()
+    m = oracle.OracleModel.from_xml(os.path.join(golden, "gap_water", "GAP.xml"))
+    args = (at.positions, at.numbers, at.lattice, [1, 1, 1])
+    full = m.calc(*args)
+    epc = full["energy_per_coordinate"]
+    nc = len(epc)
+    e0 = full["energy"] - epc.sum()
+    f_sum = np.zeros_like(full["force"])
+    for k in range(1, nc + 1):
+        r = m.calc(*args, only_descriptor=k)
+        assert abs(r["energy"] - (e0 + epc[k - 1])) < 1e-9
+        np.testing.assert_allclose(r["energy_per_coordinate"], np.where(np.arange(nc) == k - 1, epc, 0.0), atol=1e-12)
+        f_sum += r["force"]
+    np.testing.assert_allclose(f_sum, full["force"], atol=1e-9)
+    if nc > 1:  # a value matching no coordinate evaluates none (the reference's loop skips them all)
+        assert abs(m.calc(*args, only_descriptor=0)["energy"] - e0) < 1e-12
