@@ -83,6 +83,7 @@ struct gapgpu_context {
     int graph_mode = 0;                       // 0: never, 1: capture on the second identical call
     bool autotune = true;                     // time the GEMM tile candidates of a new shape once
     int gemm_pairs = 1;                       // CTA-pair GEMM tiles: 0 off, 1 autotuner candidates, 2 only
+    bool gemm2_f16 = true;                    // TF32 path: FP16 second GEMM where the model allows it
     long long graph_hits = 0, graph_launches = 0;
     // stage timing (CUDA events): neighbour build, then the evaluation's stage boundaries
     bool timed = true, stage_valid = false, nbr_timed = false;

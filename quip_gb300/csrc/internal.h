@@ -81,6 +81,8 @@ struct Coordinate {
     uint16_t* dXhi = nullptr;   // [Mpad][Dpad] BF16 hi
     uint16_t* dXlo = nullptr;   // [Mpad][Dpad] BF16 lo
     float* dXTf32 = nullptr;    // [Dpad][Mpad] transposed operands for the second GEMM
+    uint16_t* dXTh16 = nullptr;  // [Dpad][Mpad] FP16 (coef zeta / f16_scale) x: the FP16 second GEMM's operand
+    double f16_scale = 0.0;      // S of W' = S K^(zeta-1); 0: no FP16 second GEMM for this coordinate
     uint16_t* dXThi = nullptr;
     uint16_t* dXTlo = nullptr;
     float* dcoef32 = nullptr;

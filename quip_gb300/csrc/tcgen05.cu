@@ -22,6 +22,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstring>
 #include <cmath>
 #include <vector>
@@ -36,7 +37,7 @@ namespace gapgpu {
 namespace {
 
 constexpr int BM = 128, THREADS = 192;
-constexpr int MODE_BF16X3 = 1, MODE_TF32 = 2;
+constexpr int MODE_BF16X3 = 1, MODE_TF32 = 2, MODE_F16 = 3;  // F16: both operands FP16 (CTA pairs only)
 constexpr int EPI_KERNEL = 1, EPI_STORE = 2;
 constexpr long long WAIT_LIMIT = 1LL << 24;
 constexpr int SMEM_BUDGET = 200 * 1024;
@@ -190,6 +191,8 @@ struct EpiParams {
     void* out_lo;         // W lo (bf16x3)
     double* epart;        // [rows x ntiles]: energies per 64-column block
     int ntiles;
+    int w_f16;            // EPI_KERNEL, TF32: write W' = wscale K^(zeta-1) as FP16 (for the FP16 second GEMM)
+    float wscale;
 };
 
 // Epilogue of one 32-column chunk for one row: kernel function and W store (EPI_KERNEL)
@@ -206,7 +209,7 @@ __device__ __forceinline__ void epilogue_chunk(const EpiParams& ep, int row, int
             else if (ep.izeta > 0) { km1 = 1.f; for (int t = 1; t < ep.izeta; ++t) km1 *= k; }
             else km1 = powf(k, ep.zeta - 1.f);
             e_acc += cf * km1 * k;
-            w[j] = cf * ep.zeta * km1;
+            w[j] = ep.w_f16 ? ep.wscale * km1 : cf * ep.zeta * km1;
         }
         if constexpr (MODE == MODE_BF16X3) {
             __nv_bfloat16 hi[32], lo[32];
@@ -222,6 +225,14 @@ __device__ __forceinline__ void epilogue_chunk(const EpiParams& ep, int row, int
                 __stcs(oh + q, reinterpret_cast<const uint4*>(hi)[q]);
                 __stcs(ol + q, reinterpret_cast<const uint4*>(lo)[q]);
             }
+        } else if (ep.w_f16) {
+            // W' = wscale K^(zeta-1) (coef zeta / wscale is folded into the FP16 sparse points)
+            __half h[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) h[j] = __float2half_rn(w[j]);
+            uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__half*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) __stcs(o + q, reinterpret_cast<const uint4*>(h)[q]);
         } else {
             float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(ep.out_hi) + (size_t)row * ep.ldo + col0);
 #pragma unroll
@@ -253,7 +264,28 @@ __device__ __forceinline__ void epilogue_chunk_staged(const EpiParams& ep, int r
             else if (ep.izeta > 0) { km1 = 1.f; for (int t = 1; t < ep.izeta; ++t) km1 *= k; }
             else km1 = powf(k, ep.zeta - 1.f);
             e_acc += cf * km1 * k;
-            w[j] = round_tf32(cf * ep.zeta * km1);
+            w[j] = ep.w_f16 ? ep.wscale * km1 : round_tf32(cf * ep.zeta * km1);
+        }
+        if (ep.w_f16) {
+            // W' rows of 32 FP16 values (64 bytes): 16-byte chunk c of row r at c ^ ((r >> 1) & 3)
+            // (conflict-free), then every store instruction writes 8 rows x 64 contiguous bytes
+            __half h[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) h[j] = __float2half_rn(w[j]);
+            uint4* hrow = reinterpret_cast<uint4*>(reinterpret_cast<char*>(stg) + lane * 64);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) hrow[c ^ ((lane >> 1) & 3)] = reinterpret_cast<const uint4*>(h)[c];
+            __syncwarp();
+            __half* hout = reinterpret_cast<__half*>(ep.out_hi);
+            const int c = lane & 3;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = 8 * i + (lane >> 2);
+                const uint4 val = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(stg) + r * 64)[c ^ ((r >> 1) & 3)];
+                if (row0 + r < ep.rows) __stcs(reinterpret_cast<uint4*>(hout + (size_t)(row0 + r) * ep.ldo + col0) + c, val);
+            }
+            __syncwarp();
+            return;
         }
     } else {
 #pragma unroll
@@ -438,13 +470,21 @@ __device__ __forceinline__ void tma_load_pair(void* dst, const CUtensorMap* tm, 
         "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(bar_cluster), "l"(policy)
         : "memory");
 }
-// as idesc<MODE_TF32, n> with M = 256 (bits 24-28: M >> 4); the tile width n is a run-time value
+// F32 accumulator, A/B format TF32 (2, kind::tf32) or F16 (0, kind::f16), K-major, N >> 3
+// at bits 17-22, M = 256 (bits 24-28: M >> 4); the tile width n is a run-time value
+template <int MODE>
 __device__ __forceinline__ uint32_t idesc_pair(int n) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+    constexpr uint32_t f = MODE == MODE_TF32 ? 2u : 0u;
+    return (1u << 4) | (f << 7) | (f << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
 }
+template <int MODE>
 __device__ __forceinline__ void mma_pair(uint32_t dt, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
-                 "l"(a), "l"(b), "r"(idesc), "r"(acc));
+    if constexpr (MODE == MODE_TF32)
+        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
+                     "l"(a), "l"(b), "r"(idesc), "r"(acc));
+    else
+        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
+                     "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void commit_pair_multicast(uint64_t* bar) {
     asm volatile(
@@ -479,7 +519,7 @@ struct PairCfg {
 // columns; the last tile of a row block is N - (n_tiles - 1) BN wide (a multiple of 32):
 // each CTA still loads BN / 2 rows of B (rows past N read as zero) and the MMA takes the
 // first width / 2 of them.
-template <int EPI, int BN>
+template <int MODE, int EPI, int BN>
 __global__ void __launch_bounds__(THREADS, 1)
     k_tc_gemm_pair(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, int m_tiles, int n_tiles,
                    int group, int N, int kchunks, EpiParams ep, int* err) {
@@ -530,7 +570,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 unsigned char* st = smem + (size_t)s * C::STAGE;
                 const uint32_t fb = mapa_rank(su32(&full[s]), 0);
                 if (leader) mbar_expect_tx(&full[s], 2 * C::STAGE);
-                const int kx = kc * 32;
+                const int kx = kc * (MODE == MODE_TF32 ? 32 : 64);  // 128 bytes of K per stage
                 tma_load_pair(st, &tA, kx, m0, fb, pol_a);
                 tma_load_pair(st + C::TILE_A, &tB, kx, n0, fb, pol_b);
             }
@@ -552,7 +592,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const uint32_t acc_addr = tmem + buf * ACC_STRIDE;
             int mt, nt;
             tile_mn(tile, m_tiles, n_tiles, group, mt, nt);
-            const uint32_t id = idesc_pair(min(BN, N - nt * BN));
+            const uint32_t id = idesc_pair<MODE>(min(BN, N - nt * BN));
             for (int kc = 0; kc < kchunks; ++kc, ++it) {
                 const int s = it % S;
                 if (!mbar_wait(&full[s], (it / S) & 1, &abort_flag, err, 2)) { ok = false; break; }
@@ -561,8 +601,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const uint32_t bbase = base + C::TILE_A;
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk) {
-                    const uint32_t koff = kk * 32;  // 32 bytes (8 TF32) of K per instruction
-                    mma_pair(acc_addr, sdesc(base + koff), sdesc(bbase + koff), id, (kc > 0 || kk > 0) ? 1u : 0u);
+                    const uint32_t koff = kk * 32;  // 32 bytes (8 TF32 or 16 FP16) of K per instruction
+                    mma_pair<MODE>(acc_addr, sdesc(base + koff), sdesc(bbase + koff), id, (kc > 0 || kk > 0) ? 1u : 0u);
                 }
                 commit_pair_multicast(&empty[s]);
             }
@@ -617,6 +657,10 @@ __global__ void k_split_q(size_t n, const float* __restrict__ q, __nv_bfloat16* 
     __nv_bfloat16 h = __float2bfloat16_rn(x);
     hi[i] = h;
     lo[i] = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+__global__ void k_to_half(size_t n, const float* __restrict__ in, __half* __restrict__ out) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = __float2half_rn(in[i]);
 }
 __global__ void k_rowsum_scatter32(int nc, int ntiles, const double* __restrict__ epart, const int* __restrict__ centres,
                                    double* __restrict__ ecent, double* __restrict__ eatom) {
@@ -704,9 +748,9 @@ int pick_bn(int MODE, int N) {
 // the timing loop of IP_setup_parallel (src/Potentials/IP.f95:1092-1134) applied to
 // tile shapes.  Inside a stream capture no timing is possible: the heuristic decides.
 struct TuneKey {
-    int mode, epi, N, K, rb, pairs;
+    int mode, epi, N, K, rb, pairs, wf16;
     bool operator<(const TuneKey& o) const {
-        return std::tie(mode, epi, N, K, rb, pairs) < std::tie(o.mode, o.epi, o.N, o.K, o.rb, o.pairs);
+        return std::tie(mode, epi, N, K, rb, pairs, wf16) < std::tie(o.mode, o.epi, o.N, o.K, o.rb, o.pairs, o.wf16);
     }
 };
 // A tile choice: BN > 0 one CTA per 128-row tile, BN < 0 a CTA pair per 256-row tile of -BN columns.
@@ -727,7 +771,8 @@ int rows_bucket(int rows) {
 template <int MODE>
 std::vector<int> bn_candidates(int N, int pairs) {
     std::vector<int> c;
-    if (MODE != MODE_TF32) pairs = 0;
+    if (MODE == MODE_F16) pairs = 2;  // FP16 tiles exist on CTA pairs only
+    else if (MODE != MODE_TF32) pairs = 0;
     if (pairs < 2) {
         if (N % 256 == 0 && Cfg<MODE, 256>::STAGES >= 2) c.push_back(256);
         if (N % 192 == 0 && Cfg<MODE, 192>::STAGES >= 2) c.push_back(192);
@@ -747,12 +792,12 @@ std::vector<int> bn_candidates(int N, int pairs) {
 // the N-fastest order keeps each one in L2 until all its column blocks are done).
 int pair_tile_group(int n_tiles) { return n_tiles >= 16 ? 16 : 1; }
 
-template <int EPI, int BN>
+template <int MODE, int EPI, int BN>
 int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, int rows, int N, int kchunks, EpiParams ep,
                 int* err) {
     using Cf = PairCfg<BN>;
     const int smem = Cf::STAGES * Cf::STAGE + 4 * 4096 + 1024;  // stage ring, epilogue stages, alignment
-    GG_CUDA(cudaFuncSetAttribute(k_tc_gemm_pair<EPI, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    GG_CUDA(cudaFuncSetAttribute(k_tc_gemm_pair<MODE, EPI, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     const int m_tiles = (rows + 2 * BM - 1) / (2 * BM), n_tiles = (N + BN - 1) / BN;
     if (EPI == EPI_KERNEL) ep.ntiles = N / 64;  // energy blocks of 64 columns
     const int ntiles = m_tiles * n_tiles;
@@ -770,10 +815,10 @@ int launch_pair(gapgpu_context& c, const CUtensorMap& a, const CUtensorMap& b, i
     // persistent: as many pairs as can be resident at once (clusters stay within a GPC)
     cfg.gridDim = dim3(2 * (num_sms() / 2));
     int resident = 0;
-    GG_CUDA(cudaOccupancyMaxActiveClusters(&resident, k_tc_gemm_pair<EPI, BN>, &cfg));
+    GG_CUDA(cudaOccupancyMaxActiveClusters(&resident, k_tc_gemm_pair<MODE, EPI, BN>, &cfg));
     const int npairs = std::max(1, std::min(ntiles, resident > 0 ? resident : num_sms() / 2));
     cfg.gridDim = dim3(2 * npairs);
-    GG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_gemm_pair<EPI, BN>, a, b, m_tiles, n_tiles, pair_tile_group(n_tiles), N, kchunks, ep,
+    GG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_gemm_pair<MODE, EPI, BN>, a, b, m_tiles, n_tiles, pair_tile_group(n_tiles), N, kchunks, ep,
                                err));
     c.launches++;
     return GAPGPU_OK;
@@ -800,14 +845,18 @@ int launch_bn(gapgpu_context& c, const CUtensorMap& a0, const CUtensorMap& a1, c
 template <int MODE, int EPI>
 int launch_any(gapgpu_context& c, int BN, const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
                const CUtensorMap& b1, int rows, int N, int kchunks, const EpiParams& ep, int* err) {
-    if constexpr (MODE == MODE_TF32) {
-        if (BN == -256) return launch_pair<EPI, 256>(c, a0, b0, rows, N, kchunks, ep, err);
-        if (BN == -192) return launch_pair<EPI, 192>(c, a0, b0, rows, N, kchunks, ep, err);
-        if (BN == -128) return launch_pair<EPI, 128>(c, a0, b0, rows, N, kchunks, ep, err);
+    if constexpr (MODE == MODE_TF32 || MODE == MODE_F16) {
+        if (BN == -256) return launch_pair<MODE, EPI, 256>(c, a0, b0, rows, N, kchunks, ep, err);
+        if (BN == -192) return launch_pair<MODE, EPI, 192>(c, a0, b0, rows, N, kchunks, ep, err);
+        if (BN == -128 || MODE == MODE_F16) return launch_pair<MODE, EPI, 128>(c, a0, b0, rows, N, kchunks, ep, err);
     }
-    if (BN == 256) return launch_bn<MODE, EPI, 256>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
-    if (BN == 192) return launch_bn<MODE, EPI, 192>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
-    return launch_bn<MODE, EPI, 128>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+    if constexpr (MODE == MODE_F16) {
+        GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "FP16 GEMMs run on CTA pairs only");
+    } else {
+        if (BN == 256) return launch_bn<MODE, EPI, 256>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+        if (BN == 192) return launch_bn<MODE, EPI, 192>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+        return launch_bn<MODE, EPI, 128>(c, a0, a1, b0, b1, rows, N, kchunks, ep, err);
+    }
 }
 
 // One GEMM C = A B^T with the operand maps built here: A [rows x K] (planes a0, a1),
@@ -815,8 +864,10 @@ int launch_any(gapgpu_context& c, int BN, const CUtensorMap& a0, const CUtensorM
 template <int MODE, int EPI>
 int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows, int N, int K, EpiParams ep, int* err,
          int* ntiles_out) {
-    const CUtensorMapDataType dt = MODE == MODE_BF16X3 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-    const int es = MODE == MODE_BF16X3 ? 2 : 4, KB = 128 / es;
+    const CUtensorMapDataType dt = MODE == MODE_BF16X3 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                   : MODE == MODE_F16  ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                       : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const int es = MODE == MODE_TF32 ? 4 : 2, KB = 128 / es;
     const int kchunks = K / KB;
     int rc;
     auto maps = [&](int BN, CUtensorMap& a0, CUtensorMap& a1, CUtensorMap& b0, CUtensorMap& b1) {
@@ -832,8 +883,8 @@ int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows
         }
         return (int)GAPGPU_OK;
     };
-    const int pairs = MODE == MODE_TF32 ? c.gemm_pairs : 0;
-    const TuneKey key{MODE, EPI, N, K, rows_bucket(rows), pairs};
+    const int pairs = MODE == MODE_TF32 ? c.gemm_pairs : MODE == MODE_F16 ? 2 : 0;
+    const TuneKey key{MODE, EPI, N, K, rows_bucket(rows), pairs, ep.w_f16};
     int BN = 0;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -896,8 +947,12 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
         c.launches++;
     }
     const double z = co.zeta;
+    // TF32 with CTA pairs: the second GEMM in FP16 when the model's operands allow it --
+    // the first GEMM's epilogue writes W' = S K^(zeta-1) in FP16 and the sparse points carry
+    // coef zeta / S (both 10-bit mantissas, like TF32; half the W bytes, twice the MMA rate)
+    const bool f16 = MODE == MODE_TF32 && c.gemm2_f16 && c.gemm_pairs >= 1 && co.dXTh16 != nullptr;
     EpiParams ep{nc, Mp, co.dcoef32, (float)z, (z == std::floor(z) && z >= 1 && z <= 64) ? (int)z : 0, c.Wbuf.p, c.Wlo.p,
-                 c.epart.as<double>(), 0};
+                 c.epart.as<double>(), 0, f16 ? 1 : 0, (float)co.f16_scale};
     int ntiles = 0;
     // GEMM1: K = Q X^T with the kernel epilogue (W and per-tile energies)
     if (MODE == MODE_BF16X3)
@@ -911,9 +966,11 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
                                                               c.eatom.as<double>());
     c.launches++;
     // GEMM2: G = W X, B operand = X^T rows (k = sparse index contiguous)
-    EpiParams ep2{nc, Dp, nullptr, 0.f, 0, c.Gbuf.p, nullptr, nullptr, 0};
+    EpiParams ep2{nc, Dp, nullptr, 0.f, 0, c.Gbuf.p, nullptr, nullptr, 0, 0, 0.f};
     if (MODE == MODE_BF16X3)
         rc = gemm<MODE, EPI_STORE>(c, c.Wbuf.p, c.Wlo.p, co.dXThi, co.dXTlo, nc, Dp, Mp, ep2, err, nullptr);
+    else if (f16)
+        rc = gemm<MODE_F16, EPI_STORE>(c, c.Wbuf.p, c.Wbuf.p, co.dXTh16, co.dXTh16, nc, Dp, Mp, ep2, err, nullptr);
     else
         rc = gemm<MODE, EPI_STORE>(c, c.Wbuf.p, c.Wbuf.p, co.dXTf32, co.dXTf32, nc, Dp, Mp, ep2, err, nullptr);
     return rc;
@@ -969,6 +1026,37 @@ int prepare_mixed_operands(gapgpu_model& m) {
         GG_CUDA(cudaMemcpy(co.dXThi, xth.data(), 2 * ne, cudaMemcpyHostToDevice));
         GG_CUDA(cudaMemcpy(co.dXTlo, xtl.data(), 2 * ne, cudaMemcpyHostToDevice));
         GG_CUDA(cudaMemcpy(co.dcoef32, coef.data(), sizeof(float) * Mp, cudaMemcpyHostToDevice));
+        // FP16 sparse points of the FP16 second GEMM: X'[d][m] = (coef_m zeta / S) x_m[d] with
+        // S = max_m |coef_m zeta|, paired with W' = S K^(zeta-1) written by the first GEMM.  Only
+        // for integer zeta and normalised descriptors, and when S kmax^(zeta-1) stays far below
+        // the FP16 maximum (kmax: the largest possible |q.x|); otherwise the second GEMM is TF32.
+        co.f16_scale = 0.0;
+        const double zt = co.zeta;
+        double S = 0.0, xn = 0.0;
+        for (int s = 0; s < co.M; ++s) {
+            S = std::max(S, std::fabs(co.alpha[s] * co.sc[s] * co.delta * co.delta * zt));
+            double n2 = 0.0;
+            for (int d = 0; d < co.D; ++d) n2 += co.X[(size_t)s * co.D + d] * co.X[(size_t)s * co.D + d];
+            xn = std::max(xn, std::sqrt(n2));
+        }
+        const double kmax = std::sqrt(1.0 + co.soap.sigma0 * co.soap.sigma0) * xn;
+        if (zt == std::floor(zt) && zt >= 1 && zt <= 64 && co.soap.normalise && S > 0 &&
+            S * std::pow(std::max(kmax, 1.0), zt - 1) <= 1e4) {
+            std::vector<float> xs(ne, 0.f);
+            for (int s = 0; s < co.M; ++s) {
+                const double f = co.alpha[s] * co.sc[s] * co.delta * co.delta * zt / S;
+                for (int d = 0; d < co.D; ++d) xs[(size_t)d * Mp + s] = (float)(f * co.X[(size_t)s * co.D + d]);
+            }
+            float* tmp = nullptr;
+            GG_CUDA(cudaMalloc(&tmp, sizeof(float) * ne));
+            GG_CUDA(cudaMalloc(&co.dXTh16, 2 * ne));
+            GG_CUDA(cudaMemcpy(tmp, xs.data(), sizeof(float) * ne, cudaMemcpyHostToDevice));
+            k_to_half<<<(unsigned)((ne + 255) / 256), 256>>>(ne, tmp, reinterpret_cast<__half*>(co.dXTh16));
+            cudaError_t e = cudaDeviceSynchronize();
+            cudaFree(tmp);
+            if (e != cudaSuccess) GG_FAIL(GAPGPU_ERR_CUDA, std::string("FP16 operand: ") + cudaGetErrorString(e));
+            co.f16_scale = S;
+        }
     }
     return GAPGPU_OK;
 }

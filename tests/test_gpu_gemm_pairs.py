@@ -26,10 +26,11 @@ def sic_gap_tails(tmp_path_factory):
                                   atom_sigma=0.5, species=(14, 6), M=300, zeta=4.0, delta=1.0, with_2b=True, seed=3)
 
 
-def _pot(path, pairs):
+def _pot(path, pairs, f16=0):
     from quip_gb300.potential import Potential
     pot = Potential(param_filename=path, precision="tf32")
     pot.set_option("pairs", pairs)
+    pot.set_option("gemm2_f16", f16)  # tile tests: the TF32 second GEMM on both sides
     return pot
 
 
@@ -61,3 +62,20 @@ def test_pair_tiles_in_batches_and_graph_replay(sic_gap):
     for _ in range(3):
         r = pot.calc(at)
         assert r["energy"] == ref["energy"] and np.array_equal(r["force"], ref["force"])
+
+
+@pytest.mark.parametrize("n", [37, 300])
+def test_fp16_second_gemm_matches_tf32(sic_gap, n):
+    """G = W X in FP16 on CTA pairs (W' = S K^(zeta-1), X' = coef zeta / S x, both FP16 with
+    10-bit mantissas like TF32) against the TF32 second GEMM and against FP64."""
+    from quip_gb300.potential import Potential
+    at = models.random_triclinic(n, rng=np.random.default_rng(200 + n))
+    ref = _pot(sic_gap, 1, f16=0).calc(at)
+    got = _pot(sic_gap, 1, f16=1).calc(at)
+    exact = Potential(param_filename=sic_gap, precision="fp64").calc(at)
+    scale = max(1.0, np.abs(exact["force"]).max())
+    for r in (ref, got):
+        assert abs(r["energy"] - exact["energy"]) <= 1e-5 * n
+        assert np.abs(r["force"] - exact["force"]).max() <= 1e-4 * scale
+    assert np.abs(got["force"] - ref["force"]).max() <= 1e-4 * scale
+    assert got["energy"] == pytest.approx(ref["energy"], abs=1e-9 * n)  # energies come from the first GEMM
