@@ -418,6 +418,13 @@ def main():
         bound, pnote = "tensor", "of measured: cuBLAS TF32 8192^3 in this run (bf16 burst %.1f TF/s in MEASURED_PEAKS.json)" % (
             pk["bf16_tflops"])
         mult = 1.0
+        if any(t.startswith("f16 store") for t in _lib.tuning_report().splitlines()):
+            # the second GEMM ran in FP16: equal FLOPs at the TF32 and at the FP16 (= BF16) rate
+            p16 = pk["bf16_tflops"]
+            peak_tf32 = peak
+            peak = 2.0 / (1.0 / peak_tf32 + 1.0 / p16)
+            pnote = ("of measured: GEMM1 at cuBLAS TF32 8192^3 in this run (%.1f TF/s), GEMM2 (FP16) at the bf16 "
+                     "burst rate of MEASURED_PEAKS.json (%.1f TF/s); equal FLOPs, harmonic combination" % (peak_tf32, p16))
     else:
         mult = 3.0
         peak = pk["bf16_tflops"] / mult
@@ -428,10 +435,13 @@ def main():
     traffic = None
     if args.precision == "tf32" and w["kind"] == "sic":
         traffic = (790 + 216 + 644 + 48) * 1e6 * n / 8192
+    gemm2_f16 = any(t.startswith("f16 store") for t in _lib.tuning_report().splitlines())
     kernel = ("sparse-GP kernel GEMMs (FP64 SIMT k_gemm_nt_epi: K = Q X^T with fused kernel epilogue, k_gemm_nn: "
               "G = W X)" if args.precision == "fp64" else
-              "sparse-GP kernel GEMMs (tcgen05, tiles chosen by the autotuner -- k_tc_gemm_pair on CTA pairs at "
-              "this size: K = Q X^T with fused kernel epilogue, G = W X)")
+              "sparse-GP kernel GEMMs (tcgen05, tiles chosen by the autotuner: K = Q X^T in TF32 with the fused "
+              "kernel epilogue writing W' in FP16, G = W' X' in FP16 on CTA pairs)" if gemm2_f16 else
+              "sparse-GP kernel GEMMs (tcgen05, tiles chosen by the autotuner: K = Q X^T with the fused kernel "
+              "epilogue, G = W X)")
     roofline = {"bound": bound, "kernel": kernel,
                 "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s",
                 "frac": (gemm_tflops / peak) if gemm_tflops else None, "traffic": traffic,
@@ -477,7 +487,7 @@ def main():
         d2h = 8 + n * 3 * 8 + 9 * 8
         line = {"metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": world, "steps": args.steps,
                 "warmup": warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+" + args.precision,
+                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+" + args.precision + ("+f16" if gemm2_f16 else ""),
                 "data": "synthetic: seeded structures and a random GAP model (no published dataset for this path)",
                 "config": {"workload": args.workload, "precision": args.precision, "atoms": n, "sparse_points": w["M"],
                            "soap": "n_max=%d l_max=%d rc=%g species=%s" % (w["n_max"], w["l_max"], w["cutoff"],

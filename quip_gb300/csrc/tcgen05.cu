@@ -760,6 +760,7 @@ struct TuneEntry {
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneEntry> g_tune;
+std::map<TuneKey, int> g_rule;  // shapes whose tile the built-in rule chose (reported, never tuned from)
 
 int rows_bucket(int rows) {
     int b = 0;
@@ -920,7 +921,11 @@ int gemm(gapgpu_context& c, void* a0p, void* a1p, void* b0p, void* b1p, int rows
     }
     // without a timing (inside a capture, or autotuning off): 256-wide pair tiles where
     // enabled -- the fastest candidate at every row count measured on GB300
-    if (!BN) BN = pairs >= 1 ? (N >= 256 ? -256 : -128) : pick_bn(MODE, N);
+    if (!BN) {
+        BN = pairs >= 1 ? (N >= 256 ? -256 : -128) : pick_bn(MODE, N);
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_rule[key] = BN;
+    }
     CUtensorMap a0, a1, b0, b1;
     if ((rc = maps(BN, a0, a1, b0, b1))) return rc;
     if (ntiles_out) *ntiles_out = N / 64;
@@ -1080,7 +1085,8 @@ extern "C" int gapgpu_tuning_report(char* buf, int capacity) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     for (const auto& kv : g_tune) {
         const TuneKey& k = kv.first;
-        out += std::string(k.mode == MODE_BF16X3 ? "bf16x3" : "tf32") + (k.epi == EPI_KERNEL ? " kernel" : " store") +
+        out += std::string(k.mode == MODE_BF16X3 ? "bf16x3" : k.mode == MODE_F16 ? "f16" : "tf32") +
+               (k.epi == EPI_KERNEL ? (k.wf16 ? " kernel->f16" : " kernel") : " store") +
                " N=" + std::to_string(k.N) + " K=" + std::to_string(k.K) + " rows<=2^" + std::to_string(k.rb) +
                " BN=" + tile_name(kv.second.bn) + " [";
         for (size_t i = 0; i < kv.second.timings.size(); ++i) {
@@ -1090,6 +1096,14 @@ extern "C" int gapgpu_tuning_report(char* buf, int capacity) {
             out += t;
         }
         out += "]\n";
+    }
+    for (const auto& kv : g_rule) {
+        const TuneKey& k = kv.first;
+        if (g_tune.count(k)) continue;
+        out += std::string(k.mode == MODE_BF16X3 ? "bf16x3" : k.mode == MODE_F16 ? "f16" : "tf32") +
+               (k.epi == EPI_KERNEL ? (k.wf16 ? " kernel->f16" : " kernel") : " store") + " N=" + std::to_string(k.N) +
+               " K=" + std::to_string(k.K) + " rows<=2^" + std::to_string(k.rb) + " BN=" + tile_name(kv.second) +
+               " [rule]\n";
     }
     if (buf && capacity > 0) {
         std::strncpy(buf, out.c_str(), (size_t)capacity - 1);
