@@ -429,13 +429,13 @@ def main():
         mult = 3.0
         peak = pk["bf16_tflops"] / mult
         bound, pnote = "tensor", "of measured: bf16 burst %.1f TF/s / 3 (3 split-BF16 products)" % pk["bf16_tflops"]
-    # DRAM bytes of the two GEMM launches from the ncu capture of the 8192-atom case with
-    # this model (CTA-pair tiles: 790+216 MB and 644+48 MB read+written), scaled by the row
-    # count: the operand re-reads and the W/G writes grow with the rows
-    traffic = None
-    if args.precision == "tf32" and w["kind"] == "sic":
-        traffic = (790 + 216 + 644 + 48) * 1e6 * n / 8192
     gemm2_f16 = any(t.startswith("f16 store") for t in _lib.tuning_report().splitlines())
+    # DRAM bytes of the two GEMM launches from the ncu capture of the 8192-atom case with
+    # this model (CTA-pair tiles, FP16 second GEMM: 821+98 MB and 175+31 MB read+written),
+    # scaled by the row count: the operand re-reads and the W/G traffic grow with the rows
+    traffic = None
+    if args.precision == "tf32" and w["kind"] == "sic" and gemm2_f16:
+        traffic = (821 + 98 + 175 + 31) * 1e6 * n / 8192
     kernel = ("sparse-GP kernel GEMMs (FP64 SIMT k_gemm_nt_epi: K = Q X^T with fused kernel epilogue, k_gemm_nn: "
               "G = W X)" if args.precision == "fp64" else
               "sparse-GP kernel GEMMs (tcgen05, tiles chosen by the autotuner: K = Q X^T in TF32 with the fused "
