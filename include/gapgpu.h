@@ -121,7 +121,10 @@ int gapgpu_calc_batch(gapgpu_context* ctx, int nstruct, const int32_t* n_atoms, 
  * GEMM's tile candidates on the first GEMM of each new shape and keep the fastest;
  * "pairs" (0/1/2, default 1, TF32 only): GEMM tiles on CTA pairs (256-row tiles computed
  * by two SMs, tcgen05 cta_group::2) -- 0 never, 1 as autotuner candidates next to the
- * single-CTA tiles (and the choice when no timing is possible), 2 only. */
+ * single-CTA tiles (and the choice when no timing is possible), 2 only; "gemm2_f16" (0/1,
+ * default 1, TF32 with pairs): the second GEMM G = W X in FP16 (W' = S K^(zeta-1) and
+ * X' = coef zeta / S x, both 10-bit mantissas in FP16's normal range) where the model
+ * allows it (integer zeta, normalised SOAP, bounded S), else in TF32. */
 int gapgpu_context_set_option(gapgpu_context* ctx, const char* key, int value);
 
 /* energy_per_coordinate of the last gapgpu_calc / gapgpu_calc_batch whose args requested

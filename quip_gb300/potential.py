@@ -183,7 +183,8 @@ class Potential:
 
     def set_option(self, key, value):
         """Context options (gapgpu_context_set_option): graphs (CUDA-graph replay of
-        repeated shapes), timing, priority, autotune, pairs (CTA-pair GEMM tiles)."""
+        repeated shapes), timing, priority, autotune, pairs (CTA-pair GEMM tiles),
+        gemm2_f16 (the second GEMM in FP16 on the TF32 path)."""
         _lib.check(self._L.gapgpu_context_set_option(self._ctx, key.encode(), int(value)))
 
     def footprint(self, n_atoms, mean_neighbours=60.0):
