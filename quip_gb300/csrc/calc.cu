@@ -91,6 +91,10 @@ bool coordinate_chosen(const gapgpu_context& c, int k) {
     return !c.sel_coord || c.model->coords.size() <= 1 || k + 1 == c.only_coord;
 }
 
+bool gemm1_f16_active(const gapgpu_context& c, const Coordinate& co) {
+    return c.precision == GAPGPU_MIXED_TF32 && c.gemm1_f16 && c.gemm_pairs >= 1 && co.dXh16 != nullptr;
+}
+
 int upload_model(gapgpu_model& m) {
     int rc;
     if ((rc = check_device())) return rc;
@@ -125,11 +129,12 @@ void free_model_device(gapgpu_model& m) {
     m.de0 = nullptr;
     for (Coordinate& co : m.coords) {
         for (void* p : {(void*)co.dX64, (void*)co.dcoef, (void*)co.dXf32, (void*)co.dXhi, (void*)co.dXlo, (void*)co.dXTf32,
-                        (void*)co.dXThi, (void*)co.dXTlo, (void*)co.dXTh16, (void*)co.dcoef32, (void*)co.dtheta, co.dtab[0],
-                        co.dtab[1]})
+                        (void*)co.dXThi, (void*)co.dXTlo, (void*)co.dXTh16, (void*)co.dXh16, (void*)co.dcoef32,
+                        (void*)co.dtheta, co.dtab[0], co.dtab[1]})
             if (p) cudaFree(p);
         co.dtab[0] = co.dtab[1] = nullptr;
         co.dXTh16 = nullptr;
+        co.dXh16 = nullptr;
         co.dX64 = nullptr; co.dcoef = nullptr; co.dXf32 = nullptr; co.dXhi = nullptr; co.dXlo = nullptr;
         co.dXTf32 = nullptr; co.dXThi = nullptr; co.dXTlo = nullptr; co.dcoef32 = nullptr; co.dtheta = nullptr;
     }
@@ -531,6 +536,7 @@ int gapgpu_context_set_option(gapgpu_context* c, const char* key, int value) {
     else if (k == "timing") c->timed = value != 0;
     else if (k == "autotune") c->autotune = value != 0;
     else if (k == "gemm2_f16") c->gemm2_f16 = value != 0;
+    else if (k == "gemm1_f16") c->gemm1_f16 = value != 0;
     else if (k == "pairs") {
         if (value < 0 || value > 2) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_set_option: pairs must be 0, 1 or 2");
         c->gemm_pairs = value;

@@ -84,6 +84,8 @@ struct gapgpu_context {
     bool autotune = true;                     // time the GEMM tile candidates of a new shape once
     int gemm_pairs = 1;                       // CTA-pair GEMM tiles: 0 off, 1 autotuner candidates, 2 only
     bool gemm2_f16 = true;                    // TF32 path: FP16 second GEMM where the model allows it
+    bool gemm1_f16 = false;                   // ... and FP16 first GEMM (FP16 descriptors and sparse points);
+                                              // off: that GEMM is bound by its W' stores, not by the MMAs
     long long graph_hits = 0, graph_launches = 0;
     // stage timing (CUDA events): neighbour build, then the evaluation's stage boundaries
     bool timed = true, stage_valid = false, nbr_timed = false;
@@ -139,5 +141,8 @@ int pair_2b(gapgpu_context& c, const std::vector<const Coordinate*>& coords, con
 int epc_soap(gapgpu_context& c, int k, int nc, int n);
 int epc_pair(gapgpu_context& c, const Coordinate& co, int k, const int* d_mask);
 bool coordinate_chosen(const gapgpu_context& c, int k);
+// TF32 path with CTA pairs: the first GEMM K = Q X^T in FP16 (the forward kernel then writes
+// the descriptors in FP16) when the model's FP16 operands exist
+bool gemm1_f16_active(const gapgpu_context& c, const Coordinate& co);
 int gather_outputs(gapgpu_context& c, const gapgpu_model& m, int n, const int* d_mask);
 }  // namespace gapgpu

@@ -82,6 +82,7 @@ struct Coordinate {
     uint16_t* dXlo = nullptr;   // [Mpad][Dpad] BF16 lo
     float* dXTf32 = nullptr;    // [Dpad][Mpad] transposed operands for the second GEMM
     uint16_t* dXTh16 = nullptr;  // [Dpad][Mpad] FP16 (coef zeta / f16_scale) x: the FP16 second GEMM's operand
+    uint16_t* dXh16 = nullptr;   // [Mpad][Dpad] FP16 x: the FP16 first GEMM's operand
     double f16_scale = 0.0;      // S of W' = S K^(zeta-1); 0: no FP16 second GEMM for this coordinate
     uint16_t* dXThi = nullptr;
     uint16_t* dXTlo = nullptr;

@@ -22,6 +22,7 @@
 // the reference's matmul(gradPredict, grad_data(:,:,n)) (IPModel_GAP.f95:479) for the
 // neighbour entry n = j; the centre entry is minus the sum over neighbours.
 #include <cub/cub.cuh>
+#include <cuda_fp16.h>
 #include <cmath>
 #include <vector>
 #include "context.h"
@@ -446,7 +447,7 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
                                                                const int* __restrict__ centres, const int* __restrict__ Z,
                                                                const int* __restrict__ off, const int* __restrict__ nj,
                                                                const double4* __restrict__ nd, R* __restrict__ c_out,
-                                                               R* __restrict__ q_out, float* __restrict__ qr_out,
+                                                               R* __restrict__ q_out, void* __restrict__ qr_out, int qr_half,
                                                                double* __restrict__ pnorm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ci = blockIdx.x;
@@ -625,7 +626,9 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     const R inv = s_inv;
     const int np = sc.n_pairs * L;
     R* qg = q_out + (size_t)ci * sc.dpad;
-    float* qrg = qr_out ? qr_out + (size_t)ci * sc.dpad : nullptr;  // TF32-rounded copy (GEMM operand)
+    // the first GEMM's operand next to q: TF32-rounded FP32, or FP16 for the FP16 GEMM
+    float* qrg = qr_out && !qr_half ? static_cast<float*>(qr_out) + (size_t)ci * sc.dpad : nullptr;
+    __half* qhg = qr_out && qr_half ? static_cast<__half*>(qr_out) + (size_t)ci * sc.dpad : nullptr;
     for (int k = tid; k < sc.dpad; k += bd) {
         R v;
         if (k < np) v = ps[k] * inv;
@@ -633,6 +636,7 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
         else v = 0;
         qg[k] = v;
         if (qrg) __stcs(qrg + k, round_tf32((float)v));
+        if (qhg) qhg[k] = __float2half_rn((float)v);
     }
 }
 
@@ -912,7 +916,8 @@ int launch_forward_fq(gapgpu_context& c, const Coordinate& co, int nc, const Soa
     k_soap_forward<R, FQ><<<nc, FWD_THREADS, sm, c.stream>>>(sc, tab, nc, c.cur_centres, c.Z.as<int>(), c.nbr_off.as<int>(),
                                                              c.nbr_j.as<int>(), c.nbr_d.as<double4>(), c.scratch.as<R>(),
                                                              c.qbuf.as<R>(),
-                                                             c.precision == GAPGPU_MIXED_TF32 ? c.qlo.as<float>() : nullptr,
+                                                             c.precision == GAPGPU_MIXED_TF32 ? c.qlo.p : nullptr,
+                                                             gemm1_f16_active(c, co) ? 1 : 0,
                                                              c.pnorm.as<double>());
     c.launches++;
     GG_CUDA(cudaGetLastError());

@@ -959,9 +959,12 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
     EpiParams ep{nc, Mp, co.dcoef32, (float)z, (z == std::floor(z) && z >= 1 && z <= 64) ? (int)z : 0, c.Wbuf.p, c.Wlo.p,
                  c.epart.as<double>(), 0, f16 ? 1 : 0, (float)co.f16_scale};
     int ntiles = 0;
-    // GEMM1: K = Q X^T with the kernel epilogue (W and per-tile energies)
+    // GEMM1: K = Q X^T with the kernel epilogue (W and per-tile energies); in FP16 when the
+    // forward kernel wrote the descriptors in FP16
     if (MODE == MODE_BF16X3)
         rc = gemm<MODE, EPI_KERNEL>(c, c.Kbuf.p, c.qlo.p, co.dXhi, co.dXlo, nc, Mp, Dp, ep, err, &ntiles);
+    else if (gemm1_f16_active(c, co))
+        rc = gemm<MODE_F16, EPI_KERNEL>(c, c.qlo.p, c.qlo.p, co.dXh16, co.dXh16, nc, Mp, Dp, ep, err, &ntiles);
     else
         rc = gemm<MODE, EPI_KERNEL>(c, c.qlo.p, c.qlo.p, co.dXf32, co.dXf32, nc, Mp, Dp, ep, err, &ntiles);
     if (rc) return rc;
@@ -1052,14 +1055,24 @@ int prepare_mixed_operands(gapgpu_model& m) {
                 const double f = co.alpha[s] * co.sc[s] * co.delta * co.delta * zt / S;
                 for (int d = 0; d < co.D; ++d) xs[(size_t)d * Mp + s] = (float)(f * co.X[(size_t)s * co.D + d]);
             }
+            // and the unscaled sparse points of the FP16 first GEMM (normalised vectors: |x| <= xn)
+            std::vector<float> xr(ne, 0.f);
+            for (int s = 0; s < co.M; ++s)
+                for (int d = 0; d < co.D; ++d) xr[(size_t)s * Dp + d] = (float)co.X[(size_t)s * co.D + d];
             float* tmp = nullptr;
             GG_CUDA(cudaMalloc(&tmp, sizeof(float) * ne));
             GG_CUDA(cudaMalloc(&co.dXTh16, 2 * ne));
+            GG_CUDA(cudaMalloc(&co.dXh16, 2 * ne));
             GG_CUDA(cudaMemcpy(tmp, xs.data(), sizeof(float) * ne, cudaMemcpyHostToDevice));
             k_to_half<<<(unsigned)((ne + 255) / 256), 256>>>(ne, tmp, reinterpret_cast<__half*>(co.dXTh16));
             cudaError_t e = cudaDeviceSynchronize();
+            if (e == cudaSuccess) e = cudaMemcpy(tmp, xr.data(), sizeof(float) * ne, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) {
+                k_to_half<<<(unsigned)((ne + 255) / 256), 256>>>(ne, tmp, reinterpret_cast<__half*>(co.dXh16));
+                e = cudaDeviceSynchronize();
+            }
             cudaFree(tmp);
-            if (e != cudaSuccess) GG_FAIL(GAPGPU_ERR_CUDA, std::string("FP16 operand: ") + cudaGetErrorString(e));
+            if (e != cudaSuccess) GG_FAIL(GAPGPU_ERR_CUDA, std::string("FP16 operands: ") + cudaGetErrorString(e));
             co.f16_scale = S;
         }
     }

@@ -30,7 +30,8 @@ def _pot(path, pairs, f16=0):
     from quip_gb300.potential import Potential
     pot = Potential(param_filename=path, precision="tf32")
     pot.set_option("pairs", pairs)
-    pot.set_option("gemm2_f16", f16)  # tile tests: the TF32 second GEMM on both sides
+    pot.set_option("gemm2_f16", f16)  # tile tests: TF32 GEMMs on both sides
+    pot.set_option("gemm1_f16", f16)
     return pot
 
 
@@ -64,18 +65,25 @@ def test_pair_tiles_in_batches_and_graph_replay(sic_gap):
         assert r["energy"] == ref["energy"] and np.array_equal(r["force"], ref["force"])
 
 
+@pytest.mark.parametrize("g1,g2", [(0, 1), (1, 1), (1, 0)])
 @pytest.mark.parametrize("n", [37, 300])
-def test_fp16_second_gemm_matches_tf32(sic_gap, n):
-    """G = W X in FP16 on CTA pairs (W' = S K^(zeta-1), X' = coef zeta / S x, both FP16 with
-    10-bit mantissas like TF32) against the TF32 second GEMM and against FP64."""
+def test_fp16_gemms_match_tf32(sic_gap, n, g1, g2):
+    """The sparse-GP GEMMs in FP16 on CTA pairs -- K = Q X^T (FP16 descriptors and sparse
+    points) and/or G = W X (W' = S K^(zeta-1), X' = coef zeta / S x) -- against the TF32
+    GEMMs and against FP64 (FP16 and TF32 both carry 10-bit mantissas)."""
     from quip_gb300.potential import Potential
     at = models.random_triclinic(n, rng=np.random.default_rng(200 + n))
-    ref = _pot(sic_gap, 1, f16=0).calc(at)
-    got = _pot(sic_gap, 1, f16=1).calc(at)
+    ref = _pot(sic_gap, 1, f16=0)
+    ref.set_option("gemm1_f16", 0)
+    ref = ref.calc(at)
+    pot = _pot(sic_gap, 1, f16=g2)
+    pot.set_option("gemm1_f16", g1)
+    got = pot.calc(at)
     exact = Potential(param_filename=sic_gap, precision="fp64").calc(at)
     scale = max(1.0, np.abs(exact["force"]).max())
     for r in (ref, got):
         assert abs(r["energy"] - exact["energy"]) <= 1e-5 * n
         assert np.abs(r["force"] - exact["force"]).max() <= 1e-4 * scale
     assert np.abs(got["force"] - ref["force"]).max() <= 1e-4 * scale
-    assert got["energy"] == pytest.approx(ref["energy"], abs=1e-9 * n)  # energies come from the first GEMM
+    if not g1:  # energies come from the first GEMM
+        assert got["energy"] == pytest.approx(ref["energy"], abs=1e-9 * n)
