@@ -418,18 +418,24 @@ def main():
         bound, pnote = "tensor", "of measured: cuBLAS TF32 8192^3 in this run (bf16 burst %.1f TF/s in MEASURED_PEAKS.json)" % (
             pk["bf16_tflops"])
         mult = 1.0
-        if any(t.startswith("f16 store") for t in _lib.tuning_report().splitlines()):
-            # the second GEMM ran in FP16: equal FLOPs at the TF32 and at the FP16 (= BF16) rate
+        rep = _lib.tuning_report().splitlines()
+        f16_1 = any(t.startswith("f16 kernel") for t in rep)
+        f16_2 = any(t.startswith("f16 store") for t in rep)
+        if f16_1 or f16_2:
+            # GEMMs in FP16 run at the FP16 (= BF16) tensor rate; the two GEMMs have equal FLOPs
             p16 = pk["bf16_tflops"]
             peak_tf32 = peak
-            peak = 2.0 / (1.0 / peak_tf32 + 1.0 / p16)
-            pnote = ("of measured: GEMM1 at cuBLAS TF32 8192^3 in this run (%.1f TF/s), GEMM2 (FP16) at the bf16 "
-                     "burst rate of MEASURED_PEAKS.json (%.1f TF/s); equal FLOPs, harmonic combination" % (peak_tf32, p16))
+            p1, p2 = (p16 if f16_1 else peak_tf32), (p16 if f16_2 else peak_tf32)
+            peak = 2.0 / (1.0 / p1 + 1.0 / p2)
+            pnote = ("of measured: GEMM1 (%s) and GEMM2 (%s) at the bf16 burst rate of MEASURED_PEAKS.json (%.1f "
+                     "TF/s) for FP16 and cuBLAS TF32 8192^3 in this run (%.1f TF/s) for TF32; equal FLOPs, harmonic "
+                     "combination" % ("FP16" if f16_1 else "TF32", "FP16" if f16_2 else "TF32", p16, peak_tf32))
     else:
         mult = 3.0
         peak = pk["bf16_tflops"] / mult
         bound, pnote = "tensor", "of measured: bf16 burst %.1f TF/s / 3 (3 split-BF16 products)" % pk["bf16_tflops"]
     gemm2_f16 = any(t.startswith("f16 store") for t in _lib.tuning_report().splitlines())
+    gemm1_f16 = any(t.startswith("f16 kernel") for t in _lib.tuning_report().splitlines())
     # DRAM bytes of the two GEMM launches from the ncu capture of the 8192-atom case with
     # this model (CTA-pair tiles, FP16 second GEMM: 821+98 MB and 175+31 MB read+written),
     # scaled by the row count: the operand re-reads and the W/G traffic grow with the rows
@@ -438,8 +444,9 @@ def main():
         traffic = (821 + 98 + 175 + 31) * 1e6 * n / 8192
     kernel = ("sparse-GP kernel GEMMs (FP64 SIMT k_gemm_nt_epi: K = Q X^T with fused kernel epilogue, k_gemm_nn: "
               "G = W X)" if args.precision == "fp64" else
-              "sparse-GP kernel GEMMs (tcgen05, tiles chosen by the autotuner: K = Q X^T in TF32 with the fused "
-              "kernel epilogue writing W' in FP16, G = W' X' in FP16 on CTA pairs)" if gemm2_f16 else
+              "sparse-GP kernel GEMMs (tcgen05 on CTA pairs, tiles chosen by the autotuner: K = Q X^T in %s with "
+              "the fused kernel epilogue writing W' in FP16, G = W' X' in FP16)" % ("FP16" if gemm1_f16 else "TF32")
+              if gemm2_f16 else
               "sparse-GP kernel GEMMs (tcgen05, tiles chosen by the autotuner: K = Q X^T with the fused kernel "
               "epilogue, G = W X)")
     roofline = {"bound": bound, "kernel": kernel,

@@ -125,8 +125,8 @@ int gapgpu_calc_batch(gapgpu_context* ctx, int nstruct, const int32_t* n_atoms, 
  * default 1, TF32 with pairs): the second GEMM G = W X in FP16 (W' = S K^(zeta-1) and
  * X' = coef zeta / S x, both 10-bit mantissas in FP16's normal range) where the model
  * allows it (integer zeta, normalised SOAP, bounded S), else in TF32; "gemm1_f16" (0/1,
- * default 0): the first GEMM K = Q X^T in FP16 as well (FP16 descriptors from the forward
- * kernel) -- no faster on GB300, where that GEMM is bound by writing W. */
+ * default 1): the first GEMM K = Q X^T in FP16 as well (FP16 descriptors from the forward
+ * kernel and FP16 sparse points, under the same conditions). */
 int gapgpu_context_set_option(gapgpu_context* ctx, const char* key, int value);
 
 /* energy_per_coordinate of the last gapgpu_calc / gapgpu_calc_batch whose args requested

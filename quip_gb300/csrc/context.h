@@ -84,8 +84,7 @@ struct gapgpu_context {
     bool autotune = true;                     // time the GEMM tile candidates of a new shape once
     int gemm_pairs = 1;                       // CTA-pair GEMM tiles: 0 off, 1 autotuner candidates, 2 only
     bool gemm2_f16 = true;                    // TF32 path: FP16 second GEMM where the model allows it
-    bool gemm1_f16 = false;                   // ... and FP16 first GEMM (FP16 descriptors and sparse points);
-                                              // off: that GEMM is bound by its W' stores, not by the MMAs
+    bool gemm1_f16 = true;                    // ... and FP16 first GEMM (FP16 descriptors and sparse points)
     long long graph_hits = 0, graph_launches = 0;
     // stage timing (CUDA events): neighbour build, then the evaluation's stage boundaries
     bool timed = true, stage_valid = false, nbr_timed = false;

@@ -195,22 +195,42 @@ struct EpiParams {
     float wscale;
 };
 
+// Kernel function of one row's 32-column block: e += coef K^zeta and w = coef zeta K^(zeta-1)
+// (TF32-rounded when tf32_round) or W' = wscale K^(zeta-1) for the FP16 second GEMM.  The
+// zeta = 4 test is taken once per block, not per element: the unrolled common path is then
+// one contiguous stretch of code (with the other exponents interleaved per element, the
+// epilogue warps were held up by instruction fetch).
+__device__ __forceinline__ void kernel_block(const EpiParams& ep, int col0, const float* v, float& e_acc, float* w,
+                                             bool tf32_round) {
+    if (ep.izeta == 4) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float k = v[j], cf = ep.coef[col0 + j], km1 = k * k * k;
+            e_acc += cf * km1 * k;
+            const float x = cf * ep.zeta * km1;
+            w[j] = ep.w_f16 ? ep.wscale * km1 : (tf32_round ? round_tf32(x) : x);
+        }
+    } else {  // unrolled too: w and v stay in registers (this block is not executed for zeta = 4)
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float k = v[j], cf = ep.coef[col0 + j];
+            float km1;
+            if (ep.izeta > 0) { km1 = 1.f; for (int t = 1; t < ep.izeta; ++t) km1 *= k; }
+            else km1 = powf(k, ep.zeta - 1.f);
+            e_acc += cf * km1 * k;
+            const float x = cf * ep.zeta * km1;
+            w[j] = ep.w_f16 ? ep.wscale * km1 : (tf32_round ? round_tf32(x) : x);
+        }
+    }
+}
+
 // Epilogue of one 32-column chunk for one row: kernel function and W store (EPI_KERNEL)
 // or plain FP32 store (EPI_STORE).
 template <int MODE, int EPI>
 __device__ __forceinline__ void epilogue_chunk(const EpiParams& ep, int row, int col0, const float* v, float& e_acc) {
     if constexpr (EPI == EPI_KERNEL) {
         float w[32];
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const float k = v[j], cf = ep.coef[col0 + j];
-            float km1;
-            if (ep.izeta == 4) km1 = k * k * k;
-            else if (ep.izeta > 0) { km1 = 1.f; for (int t = 1; t < ep.izeta; ++t) km1 *= k; }
-            else km1 = powf(k, ep.zeta - 1.f);
-            e_acc += cf * km1 * k;
-            w[j] = ep.w_f16 ? ep.wscale * km1 : cf * ep.zeta * km1;
-        }
+        kernel_block(ep, col0, v, e_acc, w, false);
         if constexpr (MODE == MODE_BF16X3) {
             __nv_bfloat16 hi[32], lo[32];
 #pragma unroll
@@ -256,16 +276,7 @@ __device__ __forceinline__ void epilogue_chunk_staged(const EpiParams& ep, int r
                                                       float& e_acc, float* stg) {
     float w[32];
     if constexpr (EPI == EPI_KERNEL) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const float k = v[j], cf = ep.coef[col0 + j];
-            float km1;
-            if (ep.izeta == 4) km1 = k * k * k;
-            else if (ep.izeta > 0) { km1 = 1.f; for (int t = 1; t < ep.izeta; ++t) km1 *= k; }
-            else km1 = powf(k, ep.zeta - 1.f);
-            e_acc += cf * km1 * k;
-            w[j] = ep.w_f16 ? ep.wscale * km1 : round_tf32(cf * ep.zeta * km1);
-        }
+        kernel_block(ep, col0, v, e_acc, w, true);
         if (ep.w_f16) {
             // W' rows of 32 FP16 values (64 bytes): 16-byte chunk c of row r at c ^ ((r >> 1) & 3)
             // (conflict-free), then every store instruction writes 8 rows x 64 contiguous bytes
