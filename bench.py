@@ -437,11 +437,11 @@ def main():
     gemm2_f16 = any(t.startswith("f16 store") for t in _lib.tuning_report().splitlines())
     gemm1_f16 = any(t.startswith("f16 kernel") for t in _lib.tuning_report().splitlines())
     # DRAM bytes of the two GEMM launches from the ncu capture of the 8192-atom case with
-    # this model (CTA-pair tiles, FP16 second GEMM: 821+98 MB and 175+31 MB read+written),
+    # this model (CTA-pair tiles, both GEMMs in FP16: 217+87 MB and 174+32 MB read+written),
     # scaled by the row count: the operand re-reads and the W/G traffic grow with the rows
     traffic = None
-    if args.precision == "tf32" and w["kind"] == "sic" and gemm2_f16:
-        traffic = (821 + 98 + 175 + 31) * 1e6 * n / 8192
+    if args.precision == "tf32" and w["kind"] == "sic" and gemm1_f16 and gemm2_f16:
+        traffic = (217 + 87 + 174 + 32) * 1e6 * n / 8192
     kernel = ("sparse-GP kernel GEMMs (FP64 SIMT k_gemm_nt_epi: K = Q X^T with fused kernel epilogue, k_gemm_nn: "
               "G = W X)" if args.precision == "fp64" else
               "sparse-GP kernel GEMMs (tcgen05 on CTA pairs, tiles chosen by the autotuner: K = Q X^T in %s with "
