@@ -33,7 +33,8 @@ class Potential:
     Potential(args_str="IP GAP label=...", param_filename="gap.xml", precision="fp64")
 
     ``precision`` is "fp64" (plain path, matches the reference within 1e-8 eV/atom
-    and 1e-7 eV/A), "bf16x3" or "tf32" (mixed path: FP32 SOAP, tensor-core kernel GEMMs).
+    and 1e-7 eV/A), "bf16x3" or "tf32" (mixed path: FP32 SOAP, tensor-core kernel GEMMs;
+    "tf32" runs them with FP16 operands where the model allows, same 10-bit mantissas).
     """
 
     def __init__(self, args_str="", param_filename=None, param_str=None, precision="fp64"):
@@ -184,7 +185,7 @@ class Potential:
     def set_option(self, key, value):
         """Context options (gapgpu_context_set_option): graphs (CUDA-graph replay of
         repeated shapes), timing, priority, autotune, pairs (CTA-pair GEMM tiles),
-        gemm2_f16 (the second GEMM in FP16 on the TF32 path)."""
+        gemm1_f16 / gemm2_f16 (the first / second GEMM with FP16 operands on the TF32 path)."""
         _lib.check(self._L.gapgpu_context_set_option(self._ctx, key.encode(), int(value)))
 
     def footprint(self, n_atoms, mean_neighbours=60.0):
