@@ -52,7 +52,8 @@ enum gapgpu_status {
 enum gapgpu_precision {
     GAPGPU_FP64 = 0,       /* plain path: every stage in FP64 */
     GAPGPU_MIXED_BF16X3 = 1, /* SOAP in FP32, kernel GEMMs as split-BF16 (hi*hi + hi*lo + lo*hi) on tcgen05 */
-    GAPGPU_MIXED_TF32 = 2  /* SOAP in FP32, kernel GEMMs in TF32 on tcgen05 */
+    GAPGPU_MIXED_TF32 = 2  /* SOAP in FP32, kernel GEMMs on tcgen05 in TF32, or with FP16 operands (same 10-bit
+                              mantissas) where the model allows: options gemm1_f16 / gemm2_f16 */
 };
 
 /* Message of the calling thread's last error ("" if none). */
