@@ -3,14 +3,19 @@
 //   GEMM1  K = Q X^T   [nc x M]  fused epilogue: W = coef zeta K^(zeta-1) and per-tile
 //                                 row sums of coef K^zeta (the local energies)
 //   GEMM2  G = W X     [nc x D]  (dE/dq of every centre)
-// Two operand encodings, both with FP32 accumulation in TMEM:
+// Operand encodings, all with FP32 accumulation in TMEM:
 //   bf16x3: every operand is split x = hi + lo (bf16 each) and the product is
 //           hi*hi + hi*lo + lo*hi (three tcgen05.mma kind::f16 per k-step; the dropped
 //           lo*lo term is 2^-16 relative);
-//   tf32:   operands rounded to TF32 (cvt.rna), one tcgen05.mma kind::tf32 per k-step.
-// Persistent warp-specialised kernel (one CTA of 192 threads per SM, looping over the
-// output tiles of BM=128 rows x BN columns, N-fastest so that concurrent CTAs share the
-// A row block through L2):
+//   tf32:   operands rounded to TF32 (cvt.rna), one tcgen05.mma kind::tf32 per k-step;
+//   f16:    FP16 operands (the TF32 mode's default where the model allows): GEMM1 on FP16
+//           descriptors and sparse points, writing W' = S K^(zeta-1) in FP16; GEMM2 on W'
+//           and X' = (coef zeta / S) x -- 10-bit mantissas like TF32, in FP16's normal
+//           range by construction, at twice the TF32 tensor rate.
+// Two kernels: k_tc_gemm (one CTA per 128-row tile) and k_tc_gemm_pair (a cluster of two
+// CTAs per 256-row tile, tcgen05 cta_group::2; the only one for FP16), chosen per shape by
+// the autotuner.  Both are persistent and warp-specialised (192 threads, one CTA per SM,
+// looping over the output tiles):
 //   warp 0 lane 0  TMA producer: 2-D tiled loads, 128B swizzle, into an S-stage ring
 //   warp 1         TMEM owner (512 columns: two accumulator buffers); lane 0 issues
 //                  tcgen05.mma from shared-memory descriptors, tcgen05.commit frees each
