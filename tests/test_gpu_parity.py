@@ -141,6 +141,55 @@ def test_neighbour_list_matches_oracle(si_gap):
             assert g == o
 
 
+def _cubic_grid(n=4, a=2.5):
+    g = np.stack(np.meshgrid(range(n), range(n), range(n), indexing="ij"), -1).reshape(-1, 3) * a
+    return models.Atoms(np.full(len(g), 14), g, lattice=np.eye(3) * (n * a))
+
+
+def _faces_and_outside():
+    """Atoms on cell faces (fractional 0.5, -0.5, 1.0), at the largest double below 0.5,
+    and several cells outside the cell, where the wrap map_shift = -floor(s + 0.5)
+    (Connection.f95:1573-1579) decides the shifts."""
+    frac = np.array([[0.5, 0.5, 0.5], [-0.5, 0.0, 0.25], [1.0, 1.0, 0.5], [0.0, 0.0, 0.0],
+                     [3.7, -2.2, np.nextafter(0.5, 0.0)], [0.5, -0.5, 1.25], [-1.0, 2.0, -2.75],
+                     [0.25, 0.75, 0.125]])
+    lat = np.array([[6.0, 0.0, 0.0], [1.5, 5.5, 0.0], [-1.0, 0.75, 7.0]]).T
+    return models.Atoms(np.full(len(frac), 14), frac @ lat.T, lattice=lat)
+
+
+def _same_lists(got, ref, n):
+    off, j, sh = got
+    o_off, o_j, o_sh = ref[:3]
+    np.testing.assert_array_equal(np.diff(off), np.diff(o_off))
+    for a in range(n):
+        g = sorted((int(j[p]),) + tuple(sh[p]) for p in range(off[a], off[a + 1]))
+        o = sorted((int(o_j[p]),) + tuple(o_sh[p]) for p in range(o_off[a], o_off[a + 1]))
+        assert g == o
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32"])
+def test_neighbour_list_edges(si_gap, precision):
+    """Pairs exactly at the cutoff are out (strict <, Connection.f95:517) and the next
+    double above brings them in: on a 2.5 A cubic grid the shells at 2.5, 3.54 and 4.33 A
+    give 26 neighbours below 5.0 A and the 5.0 A shell 6 more.  The FP32 pre-test of the
+    mixed build leaves these exact-distance pairs to the FP64 test, so both precisions
+    give the same lists."""
+    pot = _pot(si_gap, precision)
+    grid = _cubic_grid()
+    for rc, count in ((5.0, 26), (np.nextafter(5.0, 0.0), 26), (np.nextafter(5.0, 6.0), 32),
+                      (2.5, 0), (np.nextafter(2.5, 3.0), 6)):
+        got = pot.neighbours(grid, float(rc))
+        assert set(np.diff(got[0]).tolist()) == {count}, rc
+        _same_lists(got, oracle.neighbours(grid.positions, grid.lattice, [1, 1, 1], float(rc)), len(grid))
+    at = _faces_and_outside()
+    for rc in (4.0, 7.5):
+        _same_lists(pot.neighbours(at, rc), oracle.neighbours(at.positions, at.lattice, [1, 1, 1], rc), len(at))
+
+
+def test_faces_and_outside_vs_oracle(si_gap):
+    _compare(_pot(si_gap), oracle.OracleModel.from_xml(si_gap), _faces_and_outside())
+
+
 def test_bitwise_reproducible(si_gap):
     pot = _pot(si_gap)
     at = models.si_diamond(2, rattle=0.05, seed=7)
