@@ -29,6 +29,14 @@ def test_library_exports_every_declared_symbol():
         assert re.search(r"\bT %s\b" % s, out), s
 
 
+def test_package_exports_the_quippy_style_api():
+    """The quippy-style entry points import from the package, as a quippy user writes them."""
+    from quip_gb300 import Atoms, Potential, read_xyz, write_xyz
+    for name in ("calc", "calculate", "calc_batch", "cutoff", "neighbours", "descriptors"):
+        assert callable(getattr(Potential, name)), name
+    assert callable(read_xyz) and callable(write_xyz) and Atoms is models.Atoms
+
+
 def test_bad_xml_is_rejected_before_device_use():
     L = _lib.load()
     h = ctypes.c_void_p()
