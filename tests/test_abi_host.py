@@ -46,6 +46,37 @@ def test_bad_xml_is_rejected_before_device_use():
     assert b"mismatched" in L.gapgpu_last_error() or b"parse" in L.gapgpu_last_error()
 
 
+C_HOST = r"""
+#include "gapgpu.h"
+#include <stdio.h>
+#include <string.h>
+int main(void) {
+    gapgpu_model* m = NULL;
+    const char* xml = "<GAP><GAP_params label='a'><gpSparse></GAP_params>";
+    int rc = gapgpu_model_create(xml, strlen(xml), "", ".", &m);
+    printf("%d %s\n", rc, gapgpu_last_error());
+    return (rc == GAPGPU_ERR_XML && m == NULL) ? 0 : 1;
+}
+"""
+
+
+def test_header_serves_a_plain_c_host(tmp_path):
+    """include/gapgpu.h compiles as strict C99 and a C program links against
+    libgapgpu.so and gets a status and a message back (no GPU call)."""
+    _lib.load()
+    src = tmp_path / "host.c"
+    src.write_text(C_HOST)
+    exe = str(tmp_path / "host")
+    build = lambda *a: subprocess.run(list(a), capture_output=True, text=True)  # noqa: E731
+    r = build("gcc", "-std=c99", "-pedantic", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+              str(src), "-L", os.path.dirname(_lib.LIB_PATH), "-lgapgpu",
+              "-Wl,-rpath," + os.path.dirname(_lib.LIB_PATH), "-o", exe)
+    assert r.returncode == 0, r.stderr
+    r = build(exe)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("%d " % _lib.ERR_XML) and len(r.stdout.strip()) > 2
+
+
 def test_unsupported_descriptor_is_rejected(tmp_path):
     L = _lib.load()
     p = models.write_gap_xml(str(tmp_path / "g.xml"),
