@@ -37,7 +37,7 @@
 //                  f_gp = gradPredict.grad_data*fc + e*grad_fc, F(j) -= f_gp,
 //                  virial(j) -= (pos_n - pos_centre) (x) f_gp, e0, E_scale).
 //
-// Build: oracle/Makefile -> oracle/_build/liboracle.so (g++ -O2 -fopenmp).
+// Build: oracle/Makefile -> oracle/_build/liboracle.so (g++ -O2 -ffp-contract=off -fopenmp).
 
 #include <cmath>
 #include <cstdio>
