@@ -88,6 +88,68 @@ def test_unsupported_descriptor_is_rejected(tmp_path):
     assert rc == _lib.ERR_UNSUPPORTED
 
 
+def _water_copy(tmp_path):
+    src = os.path.join(ROOT, "tests", "golden", "gap_water")
+    for f in os.listdir(src):
+        if f.startswith("GAP.xml"):
+            (tmp_path / f).write_bytes(open(os.path.join(src, f), "rb").read())
+    return (tmp_path / "GAP.xml").read_text()
+
+
+def _truncate(path, keep):
+    lines = open(path).read().splitlines()[:keep]
+    open(path, "w").write("\n".join(lines) + "\n")
+
+
+SPX = "GAP.xml.sparseX.GAP_2018_10_7_60_14_59_24_970"
+# (case, edit of the XML text and files, init_args, expected status, message fragment)
+MODEL_CASES = [
+    ("label", lambda x, d: x, "IP GAP label=nope", "ERR_XML", "no GAP_params stanza with label 'nope'"),
+    ("missing sparseX file", lambda x, d: (os.remove(d / (SPX + "2")), x)[1], "", "ERR_XML", "cannot open sparseX file"),
+    ("short sparseX file", lambda x, d: (_truncate(d / (SPX + "3"), 5), x)[1], "", "ERR_XML", "fewer than M*D"),
+    ("signal_mean", lambda x, d: x.replace('signal_mean=".00000000000000000E+000"', 'signal_mean="0.5"', 1), "",
+     "ERR_UNSUPPORTED", "signal_mean"),
+    ("covariance_type", lambda x, d: x.replace('covariance_type="1"', 'covariance_type="3"', 1), "",
+     "ERR_UNSUPPORTED", "covariance_type 3"),
+    ("permutations", lambda x, d: x.replace('n_permutations="1"', 'n_permutations="2"', 1), "",
+     "ERR_UNSUPPORTED", "permutations"),
+    ("do_pca", lambda x, d: x.replace('<GAP_data do_core="F">', '<GAP_data do_core="F" do_pca="T">', 1), "",
+     "ERR_UNSUPPORTED", "do_pca"),
+    ("bad e0", lambda x, d: x.replace('<e0 Z="2" value=".00000000000000000E+000"/>', '<e0 Z="2" value="x"/>', 1), "",
+     "ERR_XML", "bad e0 entry"),
+    ("distance_2b dimensions", lambda x, d: x.replace('dimensions="1"', 'dimensions="2"', 1), "",
+     "ERR_XML", "dimensions=1"),
+    ("ard_se without theta", lambda x, d: x.replace("<theta>  0.10000000000000000E+001 </theta>", "", 1), "",
+     "ERR_XML", "without theta"),
+]
+
+
+@pytest.mark.parametrize("case, edit, init_args, code, fragment", MODEL_CASES, ids=[c[0] for c in MODEL_CASES])
+def test_model_loader_rejections(tmp_path, case, edit, init_args, code, fragment):
+    """GAP XML checks of the model loader (IPModel_GAP.f95:618-944 reads the same
+    stanzas), each raised before any device use, with its status and message."""
+    L = _lib.load()
+    xml = edit(_water_copy(tmp_path), tmp_path).encode()
+    h = ctypes.c_void_p()
+    rc = L.gapgpu_model_create(xml, len(xml), init_args.encode(), str(tmp_path).encode(), ctypes.byref(h))
+    assert rc == getattr(_lib, code), (rc, L.gapgpu_last_error())
+    assert fragment.encode() in L.gapgpu_last_error()
+    assert not h.value
+
+
+def test_unmodified_water_model_parses(tmp_path):
+    """The same files unmodified get past every check; without a GPU the upload then
+    fails with GAPGPU_ERR_CUDA (with one, the model is created)."""
+    L = _lib.load()
+    xml = _water_copy(tmp_path).encode()
+    h = ctypes.c_void_p()
+    rc = L.gapgpu_model_create(xml, len(xml), b"", str(tmp_path).encode(), ctypes.byref(h))
+    if rc == 0:
+        L.gapgpu_model_destroy(h)
+    else:
+        assert rc == _lib.ERR_CUDA, L.gapgpu_last_error()
+
+
 def test_no_gpu_means_loud_failure(tmp_path):
     """No CPU fallback: without a GPU, model creation fails with GAPGPU_ERR_CUDA."""
     try:
