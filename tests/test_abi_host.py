@@ -137,6 +137,41 @@ def test_model_loader_rejections(tmp_path, case, edit, init_args, code, fragment
     assert not h.value
 
 
+SOAP_BASE = "soap cutoff=4 cutoff_transition_width=1 n_max=4 l_max=4 atom_sigma=0.5 central_weight=1 " \
+            "n_species=1 species_Z={14} n_Z=1 Z={14}"
+# (case, descriptor string, dimensions written, expected status, message fragment)
+SOAP_CASES = [
+    ("valid", SOAP_BASE, 51, "ERR_CUDA", ""),
+    ("n_max", SOAP_BASE.replace("n_max=4", "n_max=17"), 51, "ERR_UNSUPPORTED", "n_max outside"),
+    ("l_max", SOAP_BASE.replace("l_max=4", "l_max=13"), 51, "ERR_UNSUPPORTED", "l_max outside"),
+    ("n_species", SOAP_BASE.replace("n_species=1", "n_species=9"), 51, "ERR_UNSUPPORTED", "n_species outside"),
+    ("diagonal_radial", SOAP_BASE + " diagonal_radial=T", 51, "ERR_UNSUPPORTED", "diagonal_radial"),
+    ("average", SOAP_BASE + " average=T", 51, "ERR_UNSUPPORTED", "option average"),
+    ("cutoff_dexp", SOAP_BASE + " cutoff_dexp=2", 51, "ERR_UNSUPPORTED", "cutoff_dexp"),
+    ("species_Z short", SOAP_BASE.replace("n_species=1", "n_species=2"), 51, "ERR_XML", "species_Z shorter"),
+    ("n_Z", SOAP_BASE.replace("n_Z=1", "n_Z=2"), 51, "ERR_XML", "inconsistent n_Z"),
+    ("cutoff", SOAP_BASE.replace("cutoff=4 ", "cutoff=0 "), 51, "ERR_XML", "cutoff missing or not positive"),
+    ("dimensions", SOAP_BASE, 50, "ERR_XML", "soap dimension mismatch"),
+]
+
+
+@pytest.mark.parametrize("case, desc, D, code, fragment", SOAP_CASES, ids=[c[0] for c in SOAP_CASES])
+def test_soap_descriptor_checks(tmp_path, case, desc, D, code, fragment):
+    """The SOAP descriptor string is read with GAP's keys and defaults; options the
+    GPU path does not implement are refused rather than ignored."""
+    L = _lib.load()
+    p = models.write_gap_xml(str(tmp_path / "s.xml"), [dict(desc_str=desc, cov="dot_product", delta=1.0, zeta=2.0,
+                                                            X=np.ones((3, D)), alpha=np.ones(3), sc=np.ones(3))])
+    xml = open(p, "rb").read()
+    h = ctypes.c_void_p()
+    rc = L.gapgpu_model_create(xml, len(xml), b"", str(tmp_path).encode(), ctypes.byref(h))
+    if rc == 0 and code == "ERR_CUDA":  # a GPU is present: the valid model is created
+        L.gapgpu_model_destroy(h)
+        return
+    assert rc == getattr(_lib, code), (rc, L.gapgpu_last_error())
+    assert fragment.encode() in L.gapgpu_last_error()
+
+
 def test_unmodified_water_model_parses(tmp_path):
     """The same files unmodified get past every check; without a GPU the upload then
     fails with GAPGPU_ERR_CUDA (with one, the model is created)."""
