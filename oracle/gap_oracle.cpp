@@ -2,8 +2,8 @@
 //
 // TEST INFRASTRUCTURE ONLY.  This file is the parity oracle for the GPU library:
 // it is called by tests/, by __graft_entry__.smoke() and by the cpu_baseline /
-// `--impl reference` legs of bench.py, always as the checker or the reported CPU
-// baseline, never as part of the product path.
+// `--impl reference` legs of bench.py, always as the expected result of a comparison or
+// as the reported CPU baseline, never as part of the product path.
 //
 // Parity pins (checked by tests/test_oracle_golden.py against the reference's own
 // fixtures, copied into tests/golden/ by tests/golden/make_golden.py):
