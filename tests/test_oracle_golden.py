@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
+from quip_gb300 import models
 from quip_gb300.atoms import read_xyz
 
 SI_SOAP = ("soap atom_sigma=0.5 central_weight=1.0 cutoff=4.0 cutoff_transition_width=1.0 "
@@ -106,6 +107,40 @@ def test_oracle_forces_are_energy_gradient(golden):
         assert abs(-(e1 - e2) / (2 * h) - r["virial"][a, b]) < 1e-5
     np.testing.assert_allclose(r["local_virial"].sum(0), r["virial"], atol=1e-10)
     np.testing.assert_allclose(r["local_energy"].sum(), r["energy"], atol=1e-10)
+
+
+def _random_rotation(seed):
+    q, r = np.linalg.qr(np.random.default_rng(seed).normal(size=(3, 3)))
+    q = q * np.sign(np.diag(r))
+    return q if np.linalg.det(q) > 0 else -q
+
+
+@pytest.mark.parametrize("case", ["si_fixture", "two_species"])
+def test_oracle_rotation_covariance(golden, tmp_path, case):
+    """Rotating the atoms with their cell leaves E unchanged and rotates F (F R^T) and
+    the virial (R V R^T): checks the real spherical harmonics, the power spectrum and
+    the force/virial assembly as a whole, for one and for two species channels."""
+    if case == "si_fixture":
+        fr = read_xyz(os.path.join(golden, "Si.np1.xyz"))[4]
+        X = np.load(os.path.join(golden, "si_soap_cur_points.npz"))["sparsex"]
+        parsed = dict(e0={14: -0.5}, coords=[dict(desc_str=SI_SOAP, desc=oracle.parse_args(SI_SOAP), cov=2, delta=3.0,
+                                                  zeta=4.0, theta=None, M=100, D=325, X=X,
+                                                  alpha=np.random.default_rng(0).normal(0, 1, 100), sc=np.ones(100))])
+        m = oracle.OracleModel(parsed)
+        pos, Z, lat = fr.positions, fr.numbers, fr.lattice
+    else:
+        from helpers import sic_model
+        m = oracle.OracleModel.from_xml(sic_model(tmp_path))
+        at = models.random_triclinic(60, rng=np.random.default_rng(3))
+        pos, Z, lat = at.positions, at.numbers, at.lattice
+    R = _random_rotation(7)
+    r0 = m.calc(pos, Z, lat)
+    r1 = m.calc(pos @ R.T, Z, R @ lat)
+    n = len(Z)
+    assert abs(r1["energy"] - r0["energy"]) < 1e-10 * n
+    np.testing.assert_allclose(r1["force"], r0["force"] @ R.T, atol=1e-9)
+    np.testing.assert_allclose(r1["virial"], R @ r0["virial"] @ R.T, atol=1e-8)
+    np.testing.assert_allclose(r1["local_energy"], r0["local_energy"], atol=1e-10)
 
 
 def test_oracle_coordinate_options(golden):
