@@ -143,6 +143,32 @@ def test_oracle_rotation_covariance(golden, tmp_path, case):
     np.testing.assert_allclose(r1["local_energy"], r0["local_energy"], atol=1e-10)
 
 
+def test_oracle_permutation_and_cutoff_continuity(tmp_path):
+    """Relabelling the atoms permutes F and local energies and leaves E unchanged; a
+    neighbour crossing the SOAP cutoff changes E and F continuously (the cosine
+    transition brings fc and fc' to zero at r_c)."""
+    from helpers import sic_model
+    m = oracle.OracleModel.from_xml(sic_model(tmp_path))
+    at = models.random_triclinic(48, rng=np.random.default_rng(5))
+    perm = np.random.default_rng(6).permutation(len(at))
+    r0 = m.calc(at.positions, at.numbers, at.lattice)
+    r1 = m.calc(at.positions[perm], at.numbers[perm], at.lattice)
+    assert abs(r1["energy"] - r0["energy"]) < 1e-10 * len(at)
+    np.testing.assert_allclose(r1["force"], r0["force"][perm], atol=1e-10)
+    np.testing.assert_allclose(r1["local_energy"], r0["local_energy"][perm], atol=1e-10)
+    # Si-C dimer in a large cluster box, across the largest cutoff of the model's coordinates
+    rc = m.cutoff()
+    box = np.eye(3) * 40.0
+
+    def dimer(r):
+        return m.calc(np.array([[10.0, 10.0, 10.0], [10.0 + r, 10.0, 10.0]]), np.array([14, 6]), box, [0, 0, 0])
+
+    lo, hi = dimer(rc - 1e-7), dimer(rc + 1e-7)
+    assert abs(lo["energy"] - hi["energy"]) < 1e-9
+    assert np.abs(lo["force"] - hi["force"]).max() < 1e-6
+    assert np.abs(hi["force"]).max() == 0.0       # beyond every cutoff: no interaction
+
+
 def test_oracle_coordinate_options(golden):
     """only_descriptor and energy_per_coordinate (IPModel_GAP.f95:399-403, :462, :570) on the
     water model's distance_2b coordinates: the per-coordinate energies and the isolated-atom
