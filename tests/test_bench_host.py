@@ -25,6 +25,25 @@ def test_algorithmic_flops_per_atom(name, nu, expected):
     assert gemm == 4 * D * w["M"]          # the two kernel GEMMs: K = Q X^T and G = W X
 
 
+def test_clock_record_summary(tmp_path):
+    """The nvidia-smi record taken during the timed region (index, clocks.sm,
+    clocks.max.sm, power, active mask, hw_slowdown, hw_thermal, sw_thermal, sw_power_cap):
+    median SM clock of the first GPU's rows, its maximum, and every reason seen Active."""
+    rows = ["0, 2070, 2070, 900.1, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+            "1, 1200, 2070, 300.0, 0x0000000000000000, Active, Not Active, Not Active, Not Active",
+            "0, 2055, 2070, 1380.5, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+            "0, 2070, 2070, 1101.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active"]
+    p = tmp_path / "clocks.csv"
+    p.write_text("\n".join(rows) + "\n")
+    c = bench.Clocks(str(p))
+    s = c.summary()
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 3
+    assert s["reasons"] == ["sw_power_cap"]      # the other GPU's hw_slowdown row is not ours
+    p.write_text("")
+    assert s.keys() >= {"sm_mhz", "sm_max_mhz", "reasons"}
+    assert bench.Clocks(str(p)).summary()["sm_mhz"] is None
+
+
 class _TimedOracle:
     """Stands in for the oracle: a call costs FIXED seconds plus PER seconds per centre."""
     FIXED, PER = 0.05, 0.002
