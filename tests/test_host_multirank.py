@@ -47,3 +47,15 @@ def test_max_over_ranks_single_process():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.max_over_ranks(3.25) == 3.25
+
+
+def test_reference_arm_runs_on_rank_zero_only():
+    """Under torchrun the CPU reference arm is timed by rank 0 alone: any other rank
+    exits 0 at once and prints nothing."""
+    import subprocess
+    import sys
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1", MASTER_ADDR="127.0.0.1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "3", "--warmup", "3"], env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == ""
