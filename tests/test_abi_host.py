@@ -255,6 +255,56 @@ def test_oracle_neighbour_semantics():
     assert np.any((j[off[0]:off[1]] == 0))
 
 
+def _brute_force_pairs(pos, lat, pbc, rc):
+    """Every (i, j, shift) with |pos_j + L shift - pos_i| < rc, shift 0 along
+    non-periodic axes, the exact self at zero shift excluded: QUIP's pair set, enumerated
+    over a shift range wide enough for the cutoff (perpendicular heights of the cell)."""
+    vol = abs(np.linalg.det(lat))
+    a, b, c = lat[:, 0], lat[:, 1], lat[:, 2]
+    heights = [vol / np.linalg.norm(np.cross(b, c)), vol / np.linalg.norm(np.cross(c, a)),
+               vol / np.linalg.norm(np.cross(a, b))]
+    frac = np.linalg.solve(lat, pos.T).T
+    spread = frac.max(0) - frac.min(0)      # atoms may sit several cells apart
+    K = [int(np.ceil(rc / heights[k] + spread[k])) + 1 if pbc[k] else 0 for k in range(3)]
+    shifts = np.array(np.meshgrid(*[np.arange(-k, k + 1) for k in K], indexing="ij")).reshape(3, -1).T
+    out = set()
+    for i in range(len(pos)):
+        d = pos[None, :, :] - pos[i] + (shifts @ lat.T)[:, None, :]   # [shift, j, 3]
+        s_idx, js = np.nonzero(np.linalg.norm(d, axis=2) < rc)
+        for s, j in zip(s_idx, js):
+            if j == i and not shifts[s].any():
+                continue
+            out.add((i, int(j)) + tuple(int(x) for x in shifts[s]))
+    return out
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_oracle_neighbours_against_brute_force(seed):
+    """Random triclinic cells (lengths 2.5-8 A, angles 60-120 deg), random periodic flags,
+    atoms up to two cells outside the cell, cutoffs below and above the cell widths: the
+    oracle's list (Connection.f95 restated) is exactly the brute-force pair set."""
+    rng = np.random.default_rng(1000 + seed)
+    L = rng.uniform(2.5, 8.0, 3)
+    al, be, ga = np.radians(rng.uniform(60, 120, 3))
+    a = np.array([L[0], 0, 0])
+    b = L[1] * np.array([np.cos(ga), np.sin(ga), 0])
+    cx = np.cos(be)
+    cy = (np.cos(al) - np.cos(be) * np.cos(ga)) / np.sin(ga)
+    c = L[2] * np.array([cx, cy, np.sqrt(max(1e-3, 1 - cx * cx - cy * cy))])
+    lat = np.stack([a, b, c], axis=1)
+    n = int(rng.integers(1, 9))
+    frac = rng.uniform(-2.0, 3.0, (n, 3))
+    pbc = rng.integers(0, 2, 3)
+    if seed % 4 == 0:
+        pbc[:] = 1
+    pos = frac @ lat.T
+    rc = float(rng.uniform(1.5, 7.0))
+    off, j, sh, d, r = oracle.neighbours(pos, lat, pbc, rc)
+    got = {(i, int(j[p])) + tuple(int(x) for x in sh[p]) for i in range(n) for p in range(off[i], off[i + 1])}
+    assert len(got) == len(j)                   # no pair listed twice
+    assert got == _brute_force_pairs(pos, lat, pbc, rc)
+
+
 def test_descriptor_string_parsing():
     d = models.soap_descriptor_string(5.0, 10, 8, species=(14, 6))
     a = models.parse_descriptor(d)
