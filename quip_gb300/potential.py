@@ -195,15 +195,39 @@ class Potential:
                                                   float(mean_neighbours), _lib.ctypes.byref(b)))
         return b.value
 
-    def calculate(self, atoms, properties=("energy", "forces", "stress")):
-        """ASE-calculator view (quippy/quippy/potential.py:177-325): forces (N,3),
-        stress = -virial / volume (potential.py:281-284), energies (local)."""
-        r = self.calc(atoms, energy=True, force=True, virial=True, local_energy="energies" in properties)
+    def calculate(self, atoms, properties=("energy", "forces", "stress"), vol_per_atom=None):
+        """ASE-calculator view, as quippy's (quippy/quippy/potential.py:177-325): energy,
+        free_energy, forces (N,3) and stress = -virial / volume as a 6-vector in Voigt order
+        (xx, yy, zz, yz, xz, xy; potential.py:279-284); on request the local energies
+        ("energies") and per-atom stresses ("stresses" = -local_virial / atomic volume, the
+        atomic volume being `vol_per_atom` -- the name of a per-atom array of `atoms` or a
+        number -- else volume / N; potential.py:296-313).  The virial and the local
+        virials are kept in extra_results, where quippy keeps them."""
+        props = set(properties)
+        want_lv = "stresses" in props
+        r = self.calc(atoms, energy=True, force=True, virial=True, local_energy="energies" in props,
+                      local_virial=want_lv)
         res = {"energy": r["energy"], "free_energy": r["energy"], "forces": r["force"]}
-        res["stress"] = -r["virial"] / atoms.volume()
-        if "energies" in properties:
+        s = -r["virial"] / atoms.volume()
+        res["stress"] = np.array([s[0, 0], s[1, 1], s[2, 2], s[1, 2], s[0, 2], s[0, 1]])
+        extra = {"config": {"virial": np.array(r["virial"], copy=True)}, "atoms": {}}
+        if "energies" in props:
             res["energies"] = r["local_energy"]
+            extra["atoms"]["local_energy"] = np.array(r["local_energy"], copy=True)
+        if want_lv:
+            if vol_per_atom is None:
+                v_atom = atoms.volume() / len(atoms)
+            elif isinstance(vol_per_atom, str) and vol_per_atom in atoms.arrays:
+                v_atom = np.asarray(atoms.arrays[vol_per_atom], dtype=np.float64).reshape(-1, 1, 1)
+            else:
+                try:
+                    v_atom = float(vol_per_atom)
+                except (TypeError, ValueError):
+                    raise ValueError("volume_per_atom: not found in atoms.arrays and not a number")
+            res["stresses"] = -r["local_virial"] / v_atom
+            extra["atoms"]["local_virial"] = np.array(r["local_virial"], copy=True)
         self.results = res
+        self.extra_results = extra
         return res
 
     def get_potential_energy(self, atoms):
@@ -211,6 +235,10 @@ class Potential:
 
     def get_forces(self, atoms):
         return self.calc(atoms, energy=False, virial=False)["force"]
+
+    def get_stress(self, atoms):
+        """-virial / volume in Voigt order, as ASE's get_stress."""
+        return self.calculate(atoms, ("stress",))["stress"]
 
     # ------------------------------------------------------------------ auxiliaries
     def neighbours(self, at, cutoff=None):

@@ -37,6 +37,35 @@ def test_package_exports_the_quippy_style_api():
     assert callable(read_xyz) and callable(write_xyz) and Atoms is models.Atoms
 
 
+def test_ase_view_matches_quippy_conventions():
+    """calculate(): stress = -virial / volume in Voigt order (xx, yy, zz, yz, xz, xy) and
+    per-atom stresses = -local_virial / atomic volume, as quippy's calculator returns them
+    (quippy/quippy/potential.py:279-284, :296-313).  Host logic only: calc is stubbed."""
+    from quip_gb300 import Potential
+    rng = np.random.default_rng(2)
+    n = 4
+    at = models.Atoms(np.full(n, 14), rng.uniform(0, 5, (n, 3)), lattice=np.diag([5.0, 6.0, 7.0]))
+    at.arrays["vol"] = np.array([40.0, 50.0, 60.0, 60.0])
+    V = rng.normal(size=(3, 3))
+    LV = rng.normal(size=(n, 3, 3))
+    pot = object.__new__(Potential)
+    pot.calc = lambda a, **k: {"energy": -1.5, "force": np.ones((n, 3)), "virial": V,
+                               "local_energy": np.arange(n, dtype=float), "local_virial": LV}
+    r = pot.calculate(at, ("energy", "forces", "stress", "energies", "stresses"))
+    s = -V / 210.0
+    np.testing.assert_allclose(r["stress"], [s[0, 0], s[1, 1], s[2, 2], s[1, 2], s[0, 2], s[0, 1]])
+    np.testing.assert_allclose(r["stresses"], -LV / (210.0 / n))
+    assert r["free_energy"] == r["energy"] == -1.5 and r["energies"].shape == (n,)
+    np.testing.assert_array_equal(pot.extra_results["config"]["virial"], V)
+    np.testing.assert_array_equal(pot.extra_results["atoms"]["local_virial"], LV)
+    np.testing.assert_allclose(pot.calculate(at, ("stresses",), vol_per_atom=30.0)["stresses"], -LV / 30.0)
+    np.testing.assert_allclose(pot.calculate(at, ("stresses",), vol_per_atom="vol")["stresses"],
+                               -LV / at.arrays["vol"][:, None, None])
+    with pytest.raises(ValueError):
+        pot.calculate(at, ("stresses",), vol_per_atom="no_such_array")
+    np.testing.assert_allclose(pot.get_stress(at), r["stress"])
+
+
 def test_bad_xml_is_rejected_before_device_use():
     L = _lib.load()
     h = ctypes.c_void_p()
