@@ -195,26 +195,43 @@ class Potential:
                                                   float(mean_neighbours), _lib.ctypes.byref(b)))
         return b.value
 
-    def calculate(self, atoms, properties=("energy", "forces", "stress"), vol_per_atom=None):
-        """ASE-calculator view, as quippy's (quippy/quippy/potential.py:177-325): energy,
+    # the calculator interface of quippy's Potential (quippy/quippy/potential.py:44-62, :177-357)
+    implemented_properties = ["energy", "free_energy", "forces", "stress", "stresses", "energies"]
+    extra_properties = ["virial", "local_virial", "local_energy"]
+    _default_properties = ["energy", "forces"]
+
+    def get_default_properties(self):
+        return list(self._default_properties)
+
+    def set_default_properties(self, properties):
+        self._default_properties = list(properties)
+
+    def calculate(self, atoms, properties=None, vol_per_atom=None):
+        """ASE-calculator view, as quippy's (quippy/quippy/potential.py:177-325).  The
+        properties asked for are added to the defaults (energy, forces).  Results: energy,
         free_energy, forces (N,3) and stress = -virial / volume as a 6-vector in Voigt order
-        (xx, yy, zz, yz, xz, xy; potential.py:279-284); on request the local energies
-        ("energies") and per-atom stresses ("stresses" = -local_virial / atomic volume, the
-        atomic volume being `vol_per_atom` -- the name of a per-atom array of `atoms` or a
-        number -- else volume / N; potential.py:296-313).  The virial and the local
-        virials are kept in extra_results, where quippy keeps them."""
-        props = set(properties)
-        want_lv = "stresses" in props
-        r = self.calc(atoms, energy=True, force=True, virial=True, local_energy="energies" in props,
-                      local_virial=want_lv)
+        (xx, yy, zz, yz, xz, xy; potential.py:279-284); with "energies" the local energies;
+        with "stresses" the per-atom stresses -local_virial / atomic volume, the atomic
+        volume being `vol_per_atom` (the name of a per-atom array of `atoms`, or a number),
+        else volume / N (potential.py:296-313).  extra_results keeps the virial (3,3) and
+        the local energies (N,) and local virials (9,N, Fortran layout) as quippy does."""
+        props = set(self.get_default_properties()) | set(properties or ())
+        for prop in props:
+            if prop not in self.implemented_properties + self.extra_properties:
+                raise RuntimeError("Don't know how to calculate property '%s'" % prop)
+        want_le = bool(props & {"energies", "local_energy"})
+        want_lv = bool(props & {"stresses", "local_virial"})
+        r = self.calc(atoms, energy=True, force=True, virial=True, local_energy=want_le, local_virial=want_lv)
         res = {"energy": r["energy"], "free_energy": r["energy"], "forces": r["force"]}
         s = -r["virial"] / atoms.volume()
         res["stress"] = np.array([s[0, 0], s[1, 1], s[2, 2], s[1, 2], s[0, 2], s[0, 1]])
         extra = {"config": {"virial": np.array(r["virial"], copy=True)}, "atoms": {}}
-        if "energies" in props:
+        if want_le:
             res["energies"] = r["local_energy"]
             extra["atoms"]["local_energy"] = np.array(r["local_energy"], copy=True)
         if want_lv:
+            lv = np.asarray(r["local_virial"])                       # (N, 3, 3)
+            extra["atoms"]["local_virial"] = lv.transpose(0, 2, 1).reshape(len(lv), 9).T.copy()
             if vol_per_atom is None:
                 v_atom = atoms.volume() / len(atoms)
             elif isinstance(vol_per_atom, str) and vol_per_atom in atoms.arrays:
@@ -224,8 +241,7 @@ class Potential:
                     v_atom = float(vol_per_atom)
                 except (TypeError, ValueError):
                     raise ValueError("volume_per_atom: not found in atoms.arrays and not a number")
-            res["stresses"] = -r["local_virial"] / v_atom
-            extra["atoms"]["local_virial"] = np.array(r["local_virial"], copy=True)
+            res["stresses"] = -lv / v_atom
         self.results = res
         self.extra_results = extra
         return res
@@ -238,7 +254,24 @@ class Potential:
 
     def get_stress(self, atoms):
         """-virial / volume in Voigt order, as ASE's get_stress."""
-        return self.calculate(atoms, ("stress",))["stress"]
+        return self.calculate(atoms, ["stress"])["stress"]
+
+    def get_virial(self, atoms):
+        self.calculate(atoms, ["stress"])
+        return self.extra_results["config"]["virial"]
+
+    def get_energies(self, atoms):
+        return self.calculate(atoms, ["energies"])["energies"]
+
+    get_local_energy = get_energies
+
+    def get_stresses(self, atoms, vol_per_atom=None):
+        return self.calculate(atoms, ["stresses"], vol_per_atom=vol_per_atom)["stresses"]
+
+    def get_local_virial(self, atoms):
+        """(9, N): each atom's virial as 9 values in column-major order."""
+        self.calculate(atoms, ["local_virial"])
+        return self.extra_results["atoms"]["local_virial"]
 
     # ------------------------------------------------------------------ auxiliaries
     def neighbours(self, at, cutoff=None):

@@ -38,9 +38,11 @@ def test_package_exports_the_quippy_style_api():
 
 
 def test_ase_view_matches_quippy_conventions():
-    """calculate(): stress = -virial / volume in Voigt order (xx, yy, zz, yz, xz, xy) and
-    per-atom stresses = -local_virial / atomic volume, as quippy's calculator returns them
-    (quippy/quippy/potential.py:279-284, :296-313).  Host logic only: calc is stubbed."""
+    """The calculator interface of quippy's Potential (quippy/quippy/potential.py:44-62,
+    :177-357): stress = -virial / volume in Voigt order (xx, yy, zz, yz, xz, xy), per-atom
+    stresses = -local_virial / atomic volume, the virial (3,3) and local virials (9,N,
+    Fortran layout) in extra_results, the getters, and the property checks.  Host logic
+    only: calc is stubbed."""
     from quip_gb300 import Potential
     rng = np.random.default_rng(2)
     n = 4
@@ -51,19 +53,30 @@ def test_ase_view_matches_quippy_conventions():
     pot = object.__new__(Potential)
     pot.calc = lambda a, **k: {"energy": -1.5, "force": np.ones((n, 3)), "virial": V,
                                "local_energy": np.arange(n, dtype=float), "local_virial": LV}
-    r = pot.calculate(at, ("energy", "forces", "stress", "energies", "stresses"))
+    assert pot.get_default_properties() == ["energy", "forces"]
+    r = pot.calculate(at, ["stress", "energies", "stresses"])
     s = -V / 210.0
     np.testing.assert_allclose(r["stress"], [s[0, 0], s[1, 1], s[2, 2], s[1, 2], s[0, 2], s[0, 1]])
     np.testing.assert_allclose(r["stresses"], -LV / (210.0 / n))
     assert r["free_energy"] == r["energy"] == -1.5 and r["energies"].shape == (n,)
     np.testing.assert_array_equal(pot.extra_results["config"]["virial"], V)
-    np.testing.assert_array_equal(pot.extra_results["atoms"]["local_virial"], LV)
-    np.testing.assert_allclose(pot.calculate(at, ("stresses",), vol_per_atom=30.0)["stresses"], -LV / 30.0)
-    np.testing.assert_allclose(pot.calculate(at, ("stresses",), vol_per_atom="vol")["stresses"],
-                               -LV / at.arrays["vol"][:, None, None])
+    lv9 = pot.extra_results["atoms"]["local_virial"]
+    assert lv9.shape == (9, n)
+    for a in range(n):   # column a: atom a's virial, column-major
+        np.testing.assert_array_equal(lv9[:, a].reshape(3, 3, order="F"), LV[a])
+    np.testing.assert_allclose(pot.get_stresses(at, vol_per_atom=30.0), -LV / 30.0)
+    np.testing.assert_allclose(pot.get_stresses(at, vol_per_atom="vol"), -LV / at.arrays["vol"][:, None, None])
     with pytest.raises(ValueError):
-        pot.calculate(at, ("stresses",), vol_per_atom="no_such_array")
+        pot.get_stresses(at, vol_per_atom="no_such_array")
+    with pytest.raises(RuntimeError):
+        pot.calculate(at, ["magnetic_moments"])
     np.testing.assert_allclose(pot.get_stress(at), r["stress"])
+    np.testing.assert_array_equal(pot.get_virial(at), V)
+    np.testing.assert_array_equal(pot.get_local_virial(at), lv9)
+    np.testing.assert_array_equal(pot.get_energies(at), np.arange(n))
+    np.testing.assert_array_equal(pot.get_local_energy(at), np.arange(n))
+    pot.set_default_properties(["energy", "forces", "stress"])
+    assert "stress" in pot.get_default_properties()
 
 
 def test_bad_xml_is_rejected_before_device_use():
