@@ -27,6 +27,16 @@ def _init_args_from_xml(xml):
     return m.group(1) if m else "IP GAP"
 
 
+def _key_val_str(args):
+    """calc_args as an args string: a dict becomes key=value pairs (logicals as T/F)."""
+    if args is None:
+        return ""
+    if isinstance(args, dict):
+        fmt = lambda v: ("T" if v else "F") if isinstance(v, bool) else str(v)  # noqa: E731
+        return " ".join("%s=%s" % (k, fmt(v)) for k, v in args.items())
+    return str(args)
+
+
 class Potential:
     """GAP potential evaluated on a GB300.
 
@@ -37,7 +47,12 @@ class Potential:
     "tf32" runs them with FP16 operands where the model allows, same 10-bit mantissas).
     """
 
-    def __init__(self, args_str="", param_filename=None, param_str=None, precision="fp64"):
+    def __init__(self, args_str="", pot1=None, pot2=None, param_str=None, param_filename=None, atoms=None,
+                 calculation_always_required=False, calc_args=None, add_arrays=None, add_info=None,
+                 precision="fp64", **kwargs):
+        # quippy's signature (quippy/quippy/potential.py:64-108), plus the GPU precision
+        if pot1 is not None or pot2 is not None:
+            raise ValueError("sums of potentials (pot1, pot2) are outside this library: it evaluates 'IP GAP'")
         if (param_filename is None) == (param_str is None):
             raise ValueError("give exactly one of param_filename / param_str")
         if param_filename is not None:
@@ -64,6 +79,12 @@ class Potential:
         _lib.check(L.gapgpu_context_create(self._model, _lib.PRECISIONS[precision], _lib.ctypes.byref(c)))
         self._ctx = c
         self.results = {}
+        self.extra_results = {"config": {}, "atoms": {}}
+        self.calc_args = _key_val_str(calc_args)
+        self.calculation_always_required = calculation_always_required
+        self.add_arrays, self.add_info = add_arrays, add_info
+        if atoms is not None:
+            atoms.calc = self
 
     def __del__(self):
         L = getattr(self, "_L", None)
@@ -199,6 +220,7 @@ class Potential:
     implemented_properties = ["energy", "free_energy", "forces", "stress", "stresses", "energies"]
     extra_properties = ["virial", "local_virial", "local_energy"]
     _default_properties = ["energy", "forces"]
+    calc_args = ""
 
     def get_default_properties(self):
         return list(self._default_properties)
@@ -221,7 +243,8 @@ class Potential:
                 raise RuntimeError("Don't know how to calculate property '%s'" % prop)
         want_le = bool(props & {"energies", "local_energy"})
         want_lv = bool(props & {"stresses", "local_virial"})
-        r = self.calc(atoms, energy=True, force=True, virial=True, local_energy=want_le, local_virial=want_lv)
+        r = self.calc(atoms, energy=True, force=True, virial=True, local_energy=want_le, local_virial=want_lv,
+                      args_str=self.calc_args)
         res = {"energy": r["energy"], "free_energy": r["energy"], "forces": r["force"]}
         s = -r["virial"] / atoms.volume()
         res["stress"] = np.array([s[0, 0], s[1, 1], s[2, 2], s[1, 2], s[0, 2], s[0, 1]])

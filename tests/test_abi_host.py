@@ -79,6 +79,26 @@ def test_ase_view_matches_quippy_conventions():
     assert "stress" in pot.get_default_properties()
 
 
+def test_quippy_constructor_arguments():
+    """quippy's constructor keywords: a sum of potentials is refused; calc_args (a string,
+    or a dict written as key=value with logicals as T/F) is the args string calculate()
+    passes to calc, as quippy's calculator does."""
+    from quip_gb300 import Potential
+    from quip_gb300.potential import _key_val_str
+    with pytest.raises(ValueError, match="sums of potentials"):
+        Potential("Sum", pot1=object(), pot2=object())
+    assert _key_val_str({"only_descriptor": 2, "do_calc_connect": True}) == "only_descriptor=2 do_calc_connect=T"
+    assert _key_val_str(None) == "" and _key_val_str("a=1") == "a=1"
+    seen = []
+    pot = object.__new__(Potential)
+    pot.calc_args = _key_val_str({"energy_per_coordinate": "epc"})
+    pot.calc = lambda a, **k: (seen.append(k.get("args_str")),
+                               {"energy": 0.0, "force": np.zeros((1, 3)), "virial": np.zeros((3, 3))})[1]
+    at = models.Atoms([14], np.zeros((1, 3)), lattice=np.eye(3) * 5.0)
+    pot.calculate(at)
+    assert seen == ["energy_per_coordinate=epc"]
+
+
 def test_bad_xml_is_rejected_before_device_use():
     L = _lib.load()
     h = ctypes.c_void_p()
