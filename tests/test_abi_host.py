@@ -99,6 +99,24 @@ def test_quippy_constructor_arguments():
     assert seen == ["energy_per_coordinate=epc"]
 
 
+def test_constructor_runs_through_with_a_stub_library(monkeypatch):
+    """The whole constructor, with the library calls answered by a stub (model and
+    context created): quippy's keywords land where calculate() and ASE expect them."""
+    from quip_gb300 import Potential, potential
+
+    class _Stub:
+        def __getattr__(self, name):
+            return lambda *a: 0
+
+    monkeypatch.setattr(potential._lib, "load", lambda *a, **k: _Stub())
+    at = models.Atoms([14], np.zeros((1, 3)), lattice=np.eye(3) * 5.0)
+    pot = Potential(param_filename=os.path.join(ROOT, "tests", "golden", "gap_water", "GAP.xml"),
+                    calc_args={"only_descriptor": 1}, atoms=at, precision="tf32")
+    assert pot.args_str.startswith("IP GAP label=") and pot.precision == "tf32"
+    assert pot.calc_args == "only_descriptor=1" and at.calc is pot
+    assert pot.extra_results == {"config": {}, "atoms": {}} and pot.results == {}
+
+
 def test_bad_xml_is_rejected_before_device_use():
     L = _lib.load()
     h = ctypes.c_void_p()
