@@ -10,8 +10,8 @@
 // contributes, per directed pair p = (i -> j, d = r_j + L s - r_i), a vector
 // f_p = dE_i / dr_j.  The reference scatters F(j) -= f_p, F(i) += f_p and
 // virial(j) -= d (x) f_p.  Here each atom GATHERS over its own list using the
-// reverse-pair index (the pair j -> i of p is rev[p], with d_rev = -d bitwise), so
-// there are no floating-point atomics and the result is bit-identical run to run:
+// reverse-pair index (the pair j -> i of p is rev[p], with d_rev = -d), so there are
+// no floating-point atomics and the result is bit-identical run to run:
 //   F_a   = sum_{p in a} (f_p - f_rev(p))
 //   W_a   = sum_{p in a} d_p (x) f_rev(p)
 //   e_a   = eatom_a + sum_{p in a} (epair_p + epair_rev(p)) + e0(Z_a) [mask]
