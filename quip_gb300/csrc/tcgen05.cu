@@ -44,7 +44,9 @@ namespace {
 constexpr int BM = 128, THREADS = 192;
 constexpr int MODE_BF16X3 = 1, MODE_TF32 = 2, MODE_F16 = 3;  // F16: both operands FP16 (CTA pairs only)
 constexpr int EPI_KERNEL = 1, EPI_STORE = 2;
-constexpr long long WAIT_LIMIT = 1LL << 24;
+// Every mbarrier wait gives up after WAIT_NS of GPU time (%globaltimer), far above any
+// legitimate wait of these kernels (a pipeline stage or an accumulator buffer: microseconds).
+constexpr unsigned long long WAIT_NS = 250ull * 1000 * 1000;
 constexpr int SMEM_BUDGET = 200 * 1024;
 constexpr int TMEM_COLS = 512;   // two accumulator buffers, ACC_STRIDE columns apart
 constexpr int ACC_STRIDE = 256;
@@ -83,12 +85,24 @@ __device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait.  Gives up when the limit is reached or another thread of the CTA
-// already gave up (abort flag in shared memory).
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag, int* err, int code) {
-    for (long long i = 0; i < WAIT_LIMIT; ++i) {
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait.  Gives up after WAIT_NS nanoseconds of GPU time, or as soon as another
+// thread of the CTA has given up (abort flag in shared memory).  The clock is read every
+// 64 polls (try_wait itself may suspend the thread for a short while).
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag, int* err, int code,
+                                          unsigned long long limit_ns = WAIT_NS) {
+    if (mbar_try(b, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned i = 1;; ++i) {
         if (mbar_try(b, parity)) return true;
-        if ((i & 1023) == 1023 && *abort_flag) return false;
+        if ((i & 63) == 0) {
+            if (*abort_flag) return false;
+            if (global_ns() - t0 > limit_ns) break;
+        }
     }
     *abort_flag = 1;
     atomicOr(err, code);
@@ -96,9 +110,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile
 }
 
 // Diagnostic: one warp waits on an mbarrier that nothing arrives on, with the bounded
-// wait of the GEMM kernels and a caller-chosen iteration limit; on expiry it records the
-// error code and returns.  No asynchronous copy or MMA is in flight.
-__global__ void k_wait_probe(long long limit, int* err) {
+// wait of the GEMM kernels and a caller-chosen time limit; on expiry it records the error
+// code and returns.  No asynchronous copy or MMA is in flight.
+__global__ void k_wait_probe(unsigned long long limit_ns, int* err) {
     __shared__ __align__(8) uint64_t bar;
     __shared__ volatile int abort_flag;
     if (threadIdx.x == 0) {
@@ -107,12 +121,7 @@ __global__ void k_wait_probe(long long limit, int* err) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    for (long long i = 0; i < limit; ++i) {
-        if (mbar_try(&bar, 0)) return;  // never completes: no thread arrives
-        if (abort_flag) return;
-    }
-    abort_flag = 1;
-    atomicOr(err, 8);
+    mbar_wait(&bar, 0, &abort_flag, err, 8, limit_ns);  // on expiry: err |= 8
 }
 
 // 2-D tiled TMA load with an L2 cache policy (createpolicy): the operand every CTA
@@ -1141,14 +1150,14 @@ extern "C" int gapgpu_tuning_report(char* buf, int capacity) {
     return (int)out.size();
 }
 
-extern "C" int gapgpu_selftest_bounded_wait(gapgpu_context* c, int64_t limit) {
+extern "C" int gapgpu_selftest_bounded_wait(gapgpu_context* c, int64_t limit_us) {
     using namespace gapgpu;
-    if (!c || limit < 1 || limit > (1LL << 24)) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_selftest_bounded_wait: bad argument");
+    if (!c || limit_us < 1 || limit_us > 1000000) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_selftest_bounded_wait: bad argument");
     int rc;
     if ((rc = c->total.ensure(sizeof(int) * 4))) return rc;
     int* err = c->total.as<int>() + 3;
     GG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-    k_wait_probe<<<1, 32, 0, c->stream>>>(limit, err);
+    k_wait_probe<<<1, 32, 0, c->stream>>>(1000ull * (unsigned long long)limit_us, err);
     GG_CUDA(cudaGetLastError());
     GG_CUDA(cudaStreamSynchronize(c->stream));
     return check_device_flags(*c);

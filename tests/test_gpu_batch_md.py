@@ -9,6 +9,7 @@ trajectory with a host loop of single evaluations.
 import numpy as np
 import pytest
 
+from oracle import oracle
 from quip_gb300 import models
 
 from helpers import si_model, sic_model
@@ -38,7 +39,7 @@ def _structures():
     return s
 
 
-@pytest.mark.parametrize("prec", ["fp64", "bf16x3", "tf32"])
+@pytest.mark.parametrize("prec", ["fp64", "bf16x3", "tf32", "fp16"])
 def test_batch_is_bit_identical_to_single(sic_gap, prec):
     pot = _pot(sic_gap, prec)
     structs = _structures()
@@ -111,6 +112,41 @@ def test_md_skin_reuse_agrees_with_rebuild_every_step(si_gap):
     assert ca["graph_replays"] > 0
 
 
+def test_md_kept_list_and_forces_match_oracle(si_gap):
+    """Skin reuse against the oracle (connection_calc_dists, Connection.f95:1321-1445, under
+    the skin rule :1086-1125): step until a step keeps its list (no rebuild) after at least
+    ten steps, then compare the refreshed list's pairs inside the cutoff -- (i, j, shift)
+    and r -- with the oracle's neighbour list of the current positions, and the forces and
+    energies with oracle calculations on those positions."""
+    from quip_gb300.md import MDReplicas
+    pot = _pot(si_gap)
+    md = MDReplicas(pot, _replicas(2, 60), dt=1.0, skin=0.5, temperature=1000.0, seed=5)
+    kept = False
+    for step in range(1, 80):
+        before = md.counters()["rebuilds"]
+        md.step(1)
+        kept = md.counters()["rebuilds"] == before
+        if step >= 10 and kept:
+            break
+    assert kept and md.counters()["rebuilds"] >= 2   # rebuilt at least once after the first build
+    s = md.state()
+    off, j, sh, r = md.neighbours()
+    rc = pot.cutoff()
+    om = oracle.OracleModel.from_xml(si_gap)
+    for k, at in enumerate(_replicas(2, 60)):
+        a0, a1 = s["offsets"][k], s["offsets"][k + 1]
+        pos = s["pos"][a0:a1]
+        o_off, o_j, o_sh, _, o_r = oracle.neighbours(pos, at.lattice, [1, 1, 1], rc)
+        for a in range(a1 - a0):
+            got = {(int(j[p]) - a0,) + tuple(sh[p]): r[p] for p in range(off[a0 + a], off[a0 + a + 1]) if r[p] < rc}
+            ref = {(int(o_j[p]),) + tuple(o_sh[p]): o_r[p] for p in range(o_off[a], o_off[a + 1])}
+            assert got.keys() == ref.keys()
+            assert max(abs(got[t] - ref[t]) for t in ref) < 1e-12
+        o = om.calc(pos, at.numbers, at.lattice, [1, 1, 1])
+        assert np.abs(s["force"][a0:a1] - o["force"]).max() < 1e-7
+        assert abs(s["energy"][k] - o["energy"]) / len(at) < 1e-8
+
+
 def test_md_matches_host_verlet_loop(si_gap):
     """Five steps of the device integrator against velocity Verlet written on the host
     around single evaluations."""
@@ -176,14 +212,19 @@ def test_serving_isolates_a_bad_request(sic_gap):
 
 def test_bounded_device_wait_reports_timeout_and_context_survives(sic_gap):
     """Failure detection without a fault: a kernel waits on a barrier nothing signals;
-    the wait gives up after its bound, the host reads GAPGPU_ERR_TIMEOUT, and the same
-    context then evaluates normally."""
+    the wait gives up after its time bound (20 ms here, measured on the GPU's clock), the
+    host reads GAPGPU_ERR_TIMEOUT well within a second, and the same context then
+    evaluates normally."""
+    import time
     from quip_gb300 import _lib
     pot = _pot(sic_gap, "tf32")
     at = models.random_triclinic(40, rng=np.random.default_rng(3))
     ref = pot.calc(at)["energy"]
+    t0 = time.perf_counter()
     rc = pot._L.gapgpu_selftest_bounded_wait(pot._ctx, 20000)
+    took = time.perf_counter() - t0
     assert rc == _lib.ERR_TIMEOUT
+    assert 0.015 < took < 1.0, took
     assert b"bounded device-side" in pot._L.gapgpu_last_error()
     assert pot.calc(at)["energy"] == ref
 
