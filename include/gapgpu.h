@@ -5,7 +5,7 @@
  * (connection_calc_connect, src/libAtoms/Connection.f95:1035-1310).  Everything above
  * it -- potential_calc (src/Potentials/Potential.f95:803-996), quippy's
  * Potential.calculate (quippy/quippy/potential.py:177-325), DynamicalSystem MD -- keeps
- * its signatures; a Fortran iso_c_binding module (INTEGRATION.md) binds these symbols.
+ * its signatures; a Fortran iso_c_binding module binds these symbols.
  *
  * Conventions (all match QUIP's Fortran arrays, so no copies are needed there):
  *   pos           double[3*n]   Fortran pos(3,N): pos[3*i + k]
@@ -50,10 +50,13 @@ enum gapgpu_status {
 };
 
 enum gapgpu_precision {
-    GAPGPU_FP64 = 0,       /* plain path: every stage in FP64 */
+    GAPGPU_FP64 = 0,         /* plain path: every stage in FP64 */
     GAPGPU_MIXED_BF16X3 = 1, /* SOAP in FP32, kernel GEMMs as split-BF16 (hi*hi + hi*lo + lo*hi) on tcgen05 */
-    GAPGPU_MIXED_TF32 = 2  /* SOAP in FP32, kernel GEMMs on tcgen05 in TF32, or with FP16 operands (same 10-bit
-                              mantissas) where the model allows: options gemm1_f16 / gemm2_f16 */
+    GAPGPU_MIXED_TF32 = 2,   /* SOAP in FP32, both kernel GEMMs in TF32 on tcgen05 */
+    GAPGPU_MIXED_F16 = 3     /* SOAP in FP32, both kernel GEMMs with FP16 operands on tcgen05 (10-bit mantissas
+                                like TF32, at twice its rate) where the model allows it -- integer zeta, normalised
+                                SOAP, bounded coefficients -- and in TF32 otherwise; the same context as
+                                GAPGPU_MIXED_TF32 with the options gemm1_f16 = gemm2_f16 = 1 */
 };
 
 /* Message of the calling thread's last error ("" if none). */
@@ -88,7 +91,7 @@ void gapgpu_context_destroy(gapgpu_context* ctx);
  * is the logical property named by args_str atom_mask_name: it restricts the
  * centres (and the e0 sum) exactly as the reference does.  Recognised args keys:
  * atom_mask_name (value ignored here: pass the mask array), r_scale / E_scale
- * (rejected, as in IPModel_GAP.f95:348-350), xml_version, precision=fp64|bf16x3|tf32.
+ * (rejected, as in IPModel_GAP.f95:348-350), xml_version, precision=fp64|bf16x3|tf32|fp16.
  * Unknown keys are ignored, like param_read_line(ignore_unknown=.true.). */
 int gapgpu_calc(gapgpu_context* ctx, int n, const double* pos, const int32_t* Z, const double* lattice,
                 const int32_t* pbc, const int32_t* atom_mask, double* energy, double* local_e, double* force,
@@ -123,11 +126,12 @@ int gapgpu_calc_batch(gapgpu_context* ctx, int nstruct, const int32_t* n_atoms, 
  * "pairs" (0/1/2, default 1, TF32 only): GEMM tiles on CTA pairs (256-row tiles computed
  * by two SMs, tcgen05 cta_group::2) -- 0 never, 1 as autotuner candidates next to the
  * single-CTA tiles (and the choice when no timing is possible), 2 only; "gemm2_f16" (0/1,
- * default 1, TF32 with pairs): the second GEMM G = W X in FP16 (W' = S K^(zeta-1) and
+ * TF32 and FP16 contexts with pairs; default 1 for GAPGPU_MIXED_F16, 0 for
+ * GAPGPU_MIXED_TF32): the second GEMM G = W X in FP16 (W' = S K^(zeta-1) and
  * X' = coef zeta / S x, both 10-bit mantissas in FP16's normal range) where the model
  * allows it (integer zeta, normalised SOAP, bounded S), else in TF32; "gemm1_f16" (0/1,
- * default 1): the first GEMM K = Q X^T in FP16 as well (FP16 descriptors from the forward
- * kernel and FP16 sparse points, under the same conditions). */
+ * same defaults): the first GEMM K = Q X^T in FP16 as well (FP16 descriptors from the
+ * forward kernel and FP16 sparse points, under the same conditions). */
 int gapgpu_context_set_option(gapgpu_context* ctx, const char* key, int value);
 
 /* energy_per_coordinate of the last gapgpu_calc / gapgpu_calc_batch whose args requested
@@ -169,10 +173,17 @@ gapgpu_context* gapgpu_md_context(gapgpu_md* md);
 void gapgpu_md_destroy(gapgpu_md* md);
 
 /* Failure-detection self-test: a kernel waits on a device barrier that is never
- * signalled, with the bounded wait the tensor-core GEMMs use, `limit` polls long
- * (1..2^24).  Returns GAPGPU_ERR_TIMEOUT with a message once the wait has given up; the
- * context stays usable.  Used by the tests; no counterpart in the reference. */
-int gapgpu_selftest_bounded_wait(gapgpu_context* ctx, int64_t limit);
+ * signalled, with the bounded wait the tensor-core GEMMs use (which give up after 250 ms
+ * of GPU time), here limit_us microseconds long (1..10^6).  Returns GAPGPU_ERR_TIMEOUT with
+ * a message once the wait has given up; the context stays usable.  Used by the tests; no
+ * counterpart in the reference. */
+int gapgpu_selftest_bounded_wait(gapgpu_context* ctx, int64_t limit_us);
+
+/* Diagnostic: the FP32 FMA rate of this GPU in TFLOP/s (2 FLOP per FMA), measured with
+ * CUDA events on the context's stream by an FMA-loop kernel, scalar and packed (f32x2)
+ * FMAs, the larger of the two.  The ceiling against which the SIMT kernels' rates are
+ * reported; no counterpart in the reference. */
+int gapgpu_probe_fp32_rate(gapgpu_context* ctx, double* tflops);
 
 /* Wait for the context's stream. */
 int gapgpu_context_sync(gapgpu_context* ctx);
@@ -217,19 +228,32 @@ int gapgpu_neighbours(gapgpu_context* ctx, int n, const double* pos, const doubl
  * total: d_pos double[3n] (Fortran pos(3,N)), d_offsets int32[n+1], d_nbr_j
  * int32[capacity], d_nbr_shift int32[3*capacity] (same layout as gapgpu_neighbours).
  * *total receives the number of entries; when capacity < *total, or d_nbr_j or
- * d_nbr_shift is NULL, only d_offsets and *total are written.  The work runs on
- * cuda_stream (NULL = the legacy default stream), and the call waits for that stream
- * before it returns.
+ * d_nbr_shift is NULL, only d_offsets and *total are written.  Atoms that overlap
+ * exactly (a pair distance below 1e-10, GAPGPU_ERR_ATOMS) are detected only by a call
+ * that fills the list: a count-only call returns GAPGPU_OK with offsets for such a
+ * structure, and the error comes from the second call of the count-then-fill pattern.
+ * The work runs on cuda_stream (NULL = the legacy default stream), and the call waits
+ * for that stream and copies the count to the host before it returns, so no call of it
+ * can be made while cuda_stream is being captured into a CUDA graph.
  *
  * Limits: n <= GAPGPU_STATIC_MAX_ATOMS (GAPGPU_ERR_ARG above it).  The scratch array is
  * shared by every call in the process and keeps the previous call's contents, so calls
  * that overlap on the GPU (other host threads, other streams) race: serialise them.
  * The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress), with that device current; make that first call before any
- * stream capture begins. */
+ * (cudaGetSymbolAddress), with that device current. */
 int gapgpu_neighbours_static(int n, const double* d_pos, const double* lattice, const int32_t* pbc, double cutoff,
                              int32_t* d_offsets, int32_t* d_nbr_j, int32_t* d_nbr_shift, int64_t capacity,
                              int64_t* total, void* cuda_stream);
+
+/* The neighbour list a context holds after its last evaluation or MD step -- the
+ * connection at%connect after calc_connect or, when the list was kept on its skin,
+ * after connection_calc_dists refreshed it (Connection.f95:1086-1125, :1321-1445) --
+ * read back without rebuilding: per-atom CSR over the evaluation's atoms (structures
+ * of a batch or MD replicas concatenated, indices global), j, shift (3 per entry) and
+ * the distance r of each entry.  A list kept on a skin holds every pair within
+ * cutoff + skin.  When capacity is too small only offsets and *total are written. */
+int gapgpu_context_neighbours(gapgpu_context* ctx, int32_t* offsets, int32_t* nbr_j, int32_t* nbr_shift, double* nbr_r,
+                              int64_t capacity, int64_t* total);
 
 /* SOAP descriptors (and the sum of squares before normalisation) of every centre
  * for coordinate `coordinate` of the model: the descriptor-only path of

@@ -11,8 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libgapgpu.so")
 
 OK, ERR_ARG, ERR_XML, ERR_UNSUPPORTED, ERR_CUDA, ERR_ATOMS, ERR_TIMEOUT = range(7)
-FP64, MIXED_BF16X3, MIXED_TF32 = 0, 1, 2
-PRECISIONS = {"fp64": FP64, "bf16x3": MIXED_BF16X3, "tf32": MIXED_TF32}
+FP64, MIXED_BF16X3, MIXED_TF32, MIXED_F16 = 0, 1, 2, 3
+PRECISIONS = {"fp64": FP64, "bf16x3": MIXED_BF16X3, "tf32": MIXED_TF32, "fp16": MIXED_F16}
 
 # Every symbol declared in include/gapgpu.h.
 EXPORTS = ["gapgpu_last_error", "gapgpu_model_create", "gapgpu_model_cutoff", "gapgpu_model_info",
@@ -21,7 +21,8 @@ EXPORTS = ["gapgpu_last_error", "gapgpu_model_create", "gapgpu_model_cutoff", "g
            "gapgpu_context_timings", "gapgpu_context_launches", "gapgpu_neighbours_static", "gapgpu_calc_batch",
            "gapgpu_context_set_option", "gapgpu_model_footprint", "gapgpu_md_create", "gapgpu_md_step", "gapgpu_md_state",
            "gapgpu_md_counters", "gapgpu_md_context", "gapgpu_md_destroy", "gapgpu_tuning_report",
-           "gapgpu_selftest_bounded_wait", "gapgpu_calc_lammps", "gapgpu_energy_per_coordinate"]
+           "gapgpu_selftest_bounded_wait", "gapgpu_calc_lammps", "gapgpu_energy_per_coordinate",
+           "gapgpu_probe_fp32_rate", "gapgpu_context_neighbours"]
 
 
 class GapGpuError(RuntimeError):
@@ -86,6 +87,8 @@ def load(build_if_missing=True):
                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
     L.gapgpu_context_timings.argtypes = [c_void_p, P(c_double), c_int]
     L.gapgpu_context_launches.argtypes = [c_void_p, P(i64)]
+    L.gapgpu_probe_fp32_rate.argtypes = [c_void_p, P(c_double)]
+    L.gapgpu_context_neighbours.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, i64, P(i64)]
     L.gapgpu_energy_per_coordinate.argtypes = [c_void_p, c_void_p, c_int, P(c_int)]
     _lib = L
     return L

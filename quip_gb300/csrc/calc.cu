@@ -41,7 +41,8 @@ int parse_calc_args(const char* args, ArgOpts& o) {
         if (p == "fp64") o.precision = GAPGPU_FP64;
         else if (p == "bf16x3") o.precision = GAPGPU_MIXED_BF16X3;
         else if (p == "tf32") o.precision = GAPGPU_MIXED_TF32;
-        else GG_FAIL(GAPGPU_ERR_ARG, "precision must be fp64, bf16x3 or tf32");
+        else if (p == "fp16") o.precision = GAPGPU_MIXED_F16;
+        else GG_FAIL(GAPGPU_ERR_ARG, "precision must be fp64, bf16x3, tf32 or fp16");
     }
     for (const char* k : {"local_gap_variance", "print_gap_variance"}) {
         auto it = a.find(k);
@@ -63,6 +64,28 @@ int parse_calc_args(const char* args, ArgOpts& o) {
     o.epc = ep != a.end() && !ep->second.empty();
     return GAPGPU_OK;
 }
+
+// The precision a call's args give (precision=...), for that call only.  FP16 is the TF32
+// mode with both FP16 GEMM options on, TF32 the same mode with them off; the context's own
+// options come back when the call returns.
+struct CallPrecision {
+    gapgpu_context& c;
+    bool g1, g2;
+    int prec;
+    CallPrecision(gapgpu_context& ctx, int requested) : c(ctx), g1(ctx.gemm1_f16), g2(ctx.gemm2_f16) {
+        prec = requested < 0 ? c.precision : requested;
+        if (requested == GAPGPU_MIXED_F16) {
+            prec = GAPGPU_MIXED_TF32;
+            c.gemm1_f16 = c.gemm2_f16 = true;
+        } else if (requested == GAPGPU_MIXED_TF32) {
+            c.gemm1_f16 = c.gemm2_f16 = false;
+        }
+    }
+    ~CallPrecision() {
+        c.gemm1_f16 = g1;
+        c.gemm2_f16 = g2;
+    }
+};
 
 void apply_call_opts(gapgpu_context& c, const ArgOpts& o) {
     c.sel_coord = o.select;
@@ -292,7 +315,8 @@ std::vector<uintptr_t> graph_key(const gapgpu_context& c, int precision, const i
     std::vector<uintptr_t> k = {(uintptr_t)precision, (uintptr_t)d_mask, (uintptr_t)c.n_total, (uintptr_t)c.nstruct,
                                 (uintptr_t)c.n_pairs, (uintptr_t)c.model, (uintptr_t)c.stream,
                                 (uintptr_t)c.h_chunks.size(), (uintptr_t)c.sel_coord, (uintptr_t)(intptr_t)c.only_coord,
-                                (uintptr_t)c.want_epc};
+                                (uintptr_t)c.want_epc, (uintptr_t)c.gemm1_f16, (uintptr_t)c.gemm2_f16,
+                                (uintptr_t)c.gemm_pairs};
     for (int nc : c.nc_coord) k.push_back((uintptr_t)nc);
     for (const gapgpu::DBuf* b : c.buffers()) k.push_back((uintptr_t)b->p);
     return k;
@@ -359,6 +383,44 @@ int check_device_flags(gapgpu_context& c) {
     return GAPGPU_OK;
 }
 
+}  // namespace gapgpu
+
+namespace gapgpu {
+namespace {
+
+// FMA-rate probe: FMA_CHAINS independent chains per thread (enough to hide the FMA latency
+// at 16 warps per SM), either as scalar fma.rn.f32 or as packed fma.rn.f32x2 on pairs.
+// The sum is written only when it equals a value it cannot reach, so the loop stays.
+constexpr int FMA_CHAINS = 8;
+template <bool PACKED>
+__global__ void __launch_bounds__(512) k_fma_rate(int iters, float seed, float* out) {
+    float a[FMA_CHAINS];
+#pragma unroll
+    for (int j = 0; j < FMA_CHAINS; ++j) a[j] = seed + 1e-7f * (float)(threadIdx.x + j);
+    const float m = 0.9999999f, c = 1e-7f;
+    for (int i = 0; i < iters; ++i) {
+        if constexpr (PACKED) {
+#pragma unroll
+            for (int j = 0; j < FMA_CHAINS; j += 2) {
+                unsigned long long x, mm, cc;
+                asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(a[j]), "f"(a[j + 1]));
+                asm("mov.b64 %0, {%1, %1};" : "=l"(mm) : "f"(m));
+                asm("mov.b64 %0, {%1, %1};" : "=l"(cc) : "f"(c));
+                asm("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(x) : "l"(mm), "l"(cc));
+                asm("mov.b64 {%0, %1}, %2;" : "=f"(a[j]), "=f"(a[j + 1]) : "l"(x));
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < FMA_CHAINS; ++j) a[j] = fmaf(a[j], m, c);
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < FMA_CHAINS; ++j) s += a[j];
+    if (s == -1.0f) out[blockIdx.x] = s;
+}
+
+}  // namespace
 }  // namespace gapgpu
 
 using namespace gapgpu;
@@ -493,12 +555,14 @@ void gapgpu_model_destroy(gapgpu_model* m) {
 
 int gapgpu_context_create(const gapgpu_model* m, int precision, gapgpu_context** out) {
     if (!m || !out) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_create: NULL argument");
-    if (precision < GAPGPU_FP64 || precision > GAPGPU_MIXED_TF32) GG_FAIL(GAPGPU_ERR_ARG, "unknown precision");
+    if (precision < GAPGPU_FP64 || precision > GAPGPU_MIXED_F16) GG_FAIL(GAPGPU_ERR_ARG, "unknown precision");
     int rc;
     if ((rc = check_device())) return rc;
     gapgpu_context* c = new gapgpu_context();
     c->model = m;
-    c->precision = precision;
+    // FP16 GEMMs run inside the TF32 mode (same kernels, FP16 operands where the model allows)
+    c->precision = precision == GAPGPU_MIXED_F16 ? GAPGPU_MIXED_TF32 : precision;
+    c->gemm1_f16 = c->gemm2_f16 = precision == GAPGPU_MIXED_F16;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete c;
@@ -574,7 +638,8 @@ int gapgpu_calc(gapgpu_context* c, int n, const double* pos, const int32_t* Z, c
     int rc;
     if ((rc = parse_calc_args(args, o))) return rc;
     apply_call_opts(*c, o);
-    const int prec = o.precision >= 0 ? o.precision : c->precision;
+    const CallPrecision cp(*c, o.precision);
+    const int prec = cp.prec;
     if (n == 0) {
         if (energy) *energy = 0;
         if (virial) std::memset(virial, 0, 9 * sizeof(double));
@@ -623,7 +688,8 @@ int gapgpu_calc_batch(gapgpu_context* c, int nstruct, const int32_t* n_atoms, co
     int rc;
     if ((rc = parse_calc_args(args, o))) return rc;
     apply_call_opts(*c, o);
-    const int prec = o.precision >= 0 ? o.precision : c->precision;
+    const CallPrecision cp(*c, o.precision);
+    const int prec = cp.prec;
     long long n = 0;
     for (int s = 0; s < nstruct; ++s) {
         if (n_atoms[s] < 0) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_calc_batch: negative atom count");
@@ -741,6 +807,35 @@ int gapgpu_neighbours(gapgpu_context* c, int n, const double* pos, const double*
     return GAPGPU_OK;
 }
 
+int gapgpu_context_neighbours(gapgpu_context* c, int32_t* offsets, int32_t* nbr_j, int32_t* nbr_shift, double* nbr_r,
+                              int64_t capacity, int64_t* total) {
+    if (!c || !total) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_neighbours: NULL argument");
+    if (c->n_total <= 0) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_neighbours: the context holds no evaluation's list");
+    const int n = c->n_total;
+    const long long P = c->n_pairs;
+    GG_CUDA(cudaStreamSynchronize(c->stream));
+    *total = P;
+    if (offsets) GG_CUDA(cudaMemcpy(offsets, c->nbr_off.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+    if (capacity < P || P == 0) return GAPGPU_OK;
+    if (nbr_j) GG_CUDA(cudaMemcpy(nbr_j, c->nbr_j.p, sizeof(int) * P, cudaMemcpyDeviceToHost));
+    if (nbr_shift) {
+        std::vector<int> packed(P);
+        GG_CUDA(cudaMemcpy(packed.data(), c->nbr_s.p, sizeof(int) * P, cudaMemcpyDeviceToHost));
+        for (long long p = 0; p < P; ++p) {
+            const int sh = packed[p];
+            nbr_shift[3 * p] = (sh & 1023) - 512;
+            nbr_shift[3 * p + 1] = ((sh >> 10) & 1023) - 512;
+            nbr_shift[3 * p + 2] = ((sh >> 20) & 1023) - 512;
+        }
+    }
+    if (nbr_r) {
+        std::vector<double4> d(P);
+        GG_CUDA(cudaMemcpy(d.data(), c->nbr_d.p, sizeof(double4) * P, cudaMemcpyDeviceToHost));
+        for (long long p = 0; p < P; ++p) nbr_r[p] = d[p].w;
+    }
+    return GAPGPU_OK;
+}
+
 int gapgpu_descriptors(gapgpu_context* c, int coordinate, int n, const double* pos, const int32_t* Z, const double* lattice,
                        const int32_t* pbc, double* q, int64_t capacity, int* n_centres) {
     if (!c || n <= 0 || !pos || !Z || !lattice || !pbc) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_descriptors: bad argument");
@@ -784,6 +879,41 @@ int gapgpu_context_timings(const gapgpu_context* c, double* ms, int capacity) {
     int k = std::min(capacity, 7);
     for (int i = 0; i < k; ++i) ms[i] = v[i];
     return k;
+}
+
+int gapgpu_probe_fp32_rate(gapgpu_context* c, double* tflops) {
+    if (!c || !tflops) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_probe_fp32_rate: NULL argument");
+    int rc, dev = 0, sms = 0;
+    GG_CUDA(cudaGetDevice(&dev));
+    GG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = 4 * sms, threads = 512, iters = 1 << 16;
+    if ((rc = c->scratch.ensure(sizeof(float) * blocks))) return rc;
+    cudaEvent_t e0, e1;
+    GG_CUDA(cudaEventCreate(&e0));
+    GG_CUDA(cudaEventCreate(&e1));
+    double best = 0;
+    for (int packed = 0; packed < 2; ++packed) {
+        for (int rep = 0; rep < 3; ++rep) {  // the first launch of each form is a warm-up
+            cudaEventRecord(e0, c->stream);
+            if (packed) k_fma_rate<true><<<blocks, threads, 0, c->stream>>>(iters, 1.0f, c->scratch.as<float>());
+            else k_fma_rate<false><<<blocks, threads, 0, c->stream>>>(iters, 1.0f, c->scratch.as<float>());
+            cudaEventRecord(e1, c->stream);
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                GG_FAIL(GAPGPU_ERR_CUDA, std::string("gapgpu_probe_fp32_rate: ") + cudaGetErrorString(e));
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            const double flops = 2.0 * FMA_CHAINS * (double)iters * blocks * threads;
+            if (rep > 0 && ms > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = best;
+    return GAPGPU_OK;
 }
 
 int gapgpu_context_launches(const gapgpu_context* c, int64_t* launches) {

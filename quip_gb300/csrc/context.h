@@ -83,8 +83,8 @@ struct gapgpu_context {
     int graph_mode = 0;                       // 0: never, 1: capture on the second identical call
     bool autotune = true;                     // time the GEMM tile candidates of a new shape once
     int gemm_pairs = 1;                       // CTA-pair GEMM tiles: 0 off, 1 autotuner candidates, 2 only
-    bool gemm2_f16 = true;                    // TF32 path: FP16 second GEMM where the model allows it
-    bool gemm1_f16 = true;                    // ... and FP16 first GEMM (FP16 descriptors and sparse points)
+    bool gemm2_f16 = false;                   // TF32 mode: FP16 second GEMM where the model allows it
+    bool gemm1_f16 = false;                   // ... and FP16 first GEMM (on for GAPGPU_MIXED_F16 contexts)
     long long graph_hits = 0, graph_launches = 0;
     // stage timing (CUDA events): neighbour build, then the evaluation's stage boundaries
     bool timed = true, stage_valid = false, nbr_timed = false;

@@ -104,6 +104,21 @@ class MDReplicas:
         return {"pos": pos, "velo": velo, "force": force, "energy": E, "virial": V.reshape(-1, 3, 3).transpose(0, 2, 1),
                 "kinetic": ke, "offsets": off}
 
+    def neighbours(self):
+        """The list the replicas' context holds now (built at cutoff + skin, its distances
+        refreshed while it is kept): (offsets, j, shift, r) over all replicas' atoms."""
+        L, ctx = self._L, self.context()
+        n = int(self.n_atoms.sum())
+        off = np.zeros(n + 1, np.int32)
+        tot = _lib.ctypes.c_int64()
+        _lib.check(L.gapgpu_context_neighbours(ctx, _lib.ptr(off), None, None, None, 0, _lib.ctypes.byref(tot)))
+        j = np.zeros(tot.value, np.int32)
+        sh = np.zeros((tot.value, 3), np.int32)
+        r = np.zeros(tot.value)
+        _lib.check(L.gapgpu_context_neighbours(ctx, _lib.ptr(off), _lib.ptr(j), _lib.ptr(sh), _lib.ptr(r), tot.value,
+                                               _lib.ctypes.byref(tot)))
+        return off, j, sh, r
+
     def counters(self):
         s, r, g = _lib.ctypes.c_int64(), _lib.ctypes.c_int64(), _lib.ctypes.c_int64()
         _lib.check(self._L.gapgpu_md_counters(self._md, _lib.ctypes.byref(s), _lib.ctypes.byref(r), _lib.ctypes.byref(g)))

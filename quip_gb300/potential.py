@@ -43,8 +43,9 @@ class Potential:
     Potential(args_str="IP GAP label=...", param_filename="gap.xml", precision="fp64")
 
     ``precision`` is "fp64" (plain path, matches the reference within 1e-8 eV/atom
-    and 1e-7 eV/A), "bf16x3" or "tf32" (mixed path: FP32 SOAP, tensor-core kernel GEMMs;
-    "tf32" runs them with FP16 operands where the model allows, same 10-bit mantissas).
+    and 1e-7 eV/A) or a mixed path (FP32 SOAP, tensor-core kernel GEMMs): "bf16x3"
+    (split-BF16, three products), "tf32" (TF32 operands) or "fp16" (FP16 operands where
+    the model allows it -- the same 10-bit mantissas as TF32 at twice its rate -- else TF32).
     """
 
     def __init__(self, args_str="", pot1=None, pot2=None, param_str=None, param_filename=None, atoms=None,

@@ -23,7 +23,7 @@ def si_gap(tmp_path_factory):
     return si_model(tmp_path_factory.mktemp("si_mixed"))
 
 
-@pytest.mark.parametrize("prec", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32", "fp16"])
 def test_mixed_si64_vs_fp64(si_gap, prec):
     p64, pm = _pair(si_gap, prec)
     at = models.si_diamond(2, rattle=0.05, seed=7)
@@ -40,7 +40,7 @@ def test_mixed_si64_vs_fp64(si_gap, prec):
     assert dv < 1e-2
 
 
-@pytest.mark.parametrize("prec", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32", "fp16"])
 def test_mixed_two_species_vs_fp64(tmp_path, prec):
     p = sic_model(tmp_path)
     p64, pm = _pair(p, prec)
