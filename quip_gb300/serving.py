@@ -135,12 +135,17 @@ class Server:
         def evaluate(pot, batch):
             """The batch in one pass; if that fails (a structure the library rejects:
             overlapping atoms, NaN positions, ...), each request alone, so that only
-            the bad ones fail -- their result is {"error": message}."""
+            the bad ones fail -- their result is {"error": message}.  Once the run's
+            deadline has passed, the requests not yet retried fail with
+            {"error": "deadline"} instead of being evaluated."""
             try:
                 return pot.calc_batch([r.atoms for r in batch])
             except GapGpuError:
                 out = []
                 for r in batch:
+                    if stop.is_set():
+                        out.append({"error": "deadline"})
+                        continue
                     try:
                         out.append(pot.calc_batch([r.atoms])[0])
                     except GapGpuError as e:
@@ -183,18 +188,20 @@ class Server:
                 state["error"] = e
                 stop.set()
 
-        threads = [threading.Thread(target=feeder)] + [threading.Thread(target=worker, args=(p,)) for p in self.pots]
+        threads = [threading.Thread(target=feeder, daemon=True)]
+        threads += [threading.Thread(target=worker, args=(p,), daemon=True) for p in self.pots]
         if self.md is not None:
-            threads.append(threading.Thread(target=md_loop))
+            threads.append(threading.Thread(target=md_loop, daemon=True))
         for t in threads:
             t.start()
         deadline = time.perf_counter() + timeout
-        while any(t.is_alive() for t in threads):
-            if time.perf_counter() > deadline:
-                stop.set()
+        while any(t.is_alive() for t in threads) and time.perf_counter() < deadline:
             time.sleep(0.01)
+        stop.set()
+        # after the deadline a thread only finishes the library call it is in
         for t in threads:
-            t.join()
+            t.join(timeout=max(1.0, 0.1 * timeout))
+        stuck = sum(1 for t in threads if t.is_alive())
         wall = clock()
         if state["error"] is not None:
             raise state["error"]
@@ -206,7 +213,8 @@ class Server:
                  "p99_ms": 1e3 * float(np.percentile(lat, 99)), "mean_ms": 1e3 * float(lat.mean()),
                  "atom_evals_per_s": atoms / wall if wall > 0 else 0.0, "batches": state["batches"],
                  "mean_batch_atoms": float(np.mean(state["batch_atoms"])) if state["batch_atoms"] else 0.0,
-                 "md_steps": md_info["steps"]}
+                 "md_steps": md_info["steps"], "unfinished": sum(1 for r in reqs if r.done is None),
+                 "deadline_hit": bool(state["left"] > 0), "threads_still_running": stuck}
         if self.md is not None:
             n_md = int(self.md.n_atoms.sum())
             stats["md_atom_steps_per_s"] = md_info["steps"] * n_md / wall if wall > 0 else 0.0
