@@ -4,8 +4,9 @@ The reference's own tests hold the only golden vectors for the GAP path
 (SOAP vectors, SOAP gradients, distance_2b energies/forces, small-cell energies).
 This script copies those data files verbatim, and extracts the arrays that the
 reference keeps inline in its test sources, into small files that travel with
-the repository.  It reads the reference from REF (default /root/reference) and is
-only run by hand; tests never read the reference at run time.
+the repository.  It reads the reference checkout named by the environment variable
+QUIP_REFERENCE (required) and is only run by hand; tests never read the reference at
+run time:  QUIP_REFERENCE=<path to the QUIP checkout> python tests/golden/make_golden.py
 
 Sources:
   tests/Si.np1.xyz, tests/Si.soap.cur_points.json       (test_gapfit.py:93-95, :58)
@@ -23,11 +24,13 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("QUIP_REFERENCE", "/root/reference")
+REF = os.environ.get("QUIP_REFERENCE")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "tests")):
+        sys.exit("set QUIP_REFERENCE to the QUIP checkout (the folder that holds tests/)")
     t = os.path.join(REF, "tests")
     shutil.copy(os.path.join(t, "Si.np1.xyz"), os.path.join(OUT, "Si.np1.xyz"))
     d = json.load(open(os.path.join(t, "Si.soap.cur_points.json")))
