@@ -183,16 +183,21 @@ def cpu_model():
 
 
 CPU_KEYS = ("value", "unit", "cores", "kind", "sample", "seconds_fixed", "seconds_per_centre")
+# centres timed at the large workloads: 1/16 of the 32768-atom cell (one oracle call over all
+# 32768 centres takes about a minute on 16 cores; the per-centre cost of a 256-centre sample
+# understated it by a quarter, that of a 2048-centre sample tracks it closely)
+CPU_SAMPLE = 2048
 
 
-def cpu_reference(w, at, model_path, steps, warmup, sample_atoms=None, nthreads=None):
+def cpu_reference(w, at, model_path, steps, warmup, sample_atoms=None, nthreads=None, keep=None):
     """Times the FP64 CPU restatement (oracle) on the host cores.
 
     With a sample of centres, a call costs a part paid once per structure (the neighbour
     list of all N atoms and the set-up) plus a part per evaluated centre.  Both are timed:
     a call with no centres gives the first, the sampled call minus it the second, and the
     value is the full structure's rate N / (fixed + N * per-centre), so that the fixed
-    part is spread over all N centres as in a full evaluation, not over the sample."""
+    part is spread over all N centres as in a full evaluation, not over the sample.
+    `keep` (a dict) receives the last sampled call's results and its mask."""
     from oracle import oracle
     om = oracle.OracleModel.from_xml(model_path)
     n = len(at)
@@ -208,8 +213,10 @@ def cpu_reference(w, at, model_path, steps, warmup, sample_atoms=None, nthreads=
         ts = []
         for _ in range(reps):
             t0 = time.perf_counter()
-            om.calc(at.positions, at.numbers, at.lattice, [1, 1, 1], mask=m, nthreads=cores)
+            res = om.calc(at.positions, at.numbers, at.lattice, [1, 1, 1], mask=m, nthreads=cores)
             ts.append(time.perf_counter() - t0)
+            if keep is not None and m is mask:
+                keep["result"], keep["mask"] = res, mask
         return float(np.median(ts))
 
     for _ in range(warmup):
@@ -233,12 +240,6 @@ def cpu_reference(w, at, model_path, steps, warmup, sample_atoms=None, nthreads=
     out["seconds_fixed"] = t_fixed
     out["seconds_per_centre"] = t_centre
     return out
-
-
-def sample_mask(n, sample):
-    mask = np.zeros(n, np.int32)
-    mask[np.random.default_rng(0).choice(n, sample, replace=False)] = 1
-    return mask
 
 
 def max_over_ranks(t_local):
@@ -398,8 +399,8 @@ def reference_arm(args, w):
     at = make_structure(w)
     path = make_model(w, tmp, oracle_descriptor_fn)
     full = len(at) * w["M"] * w["n_max"] <= 4096 * 2000 * 8
-    sample = None if full else 256
-    log("reference: timing the oracle (%s)" % ("all centres" if full else "256 sampled centres"))
+    sample = None if full else CPU_SAMPLE
+    log("reference: timing the oracle (%s)" % ("all centres" if full else "%d sampled centres" % CPU_SAMPLE))
     cb = cpu_reference(w, at, path, args.steps, args.warmup, sample)
     cpu = {k: cb[k] for k in CPU_KEYS if k in cb}
     cpu["cpu_model"] = cpu_model()
@@ -701,16 +702,14 @@ def main():
     # ---- CPU baseline: the oracle on a sample of centres, and each form's error against it
     cpu = None
     if extras and not args.no_cpu_baseline:
-        sample = None if n * w["M"] <= 4096 * 2000 else 128
+        sample = None if n * w["M"] <= 4096 * 2000 else CPU_SAMPLE
         log("cpu baseline (oracle, %s)" % ("all centres" if sample is None else "%d sampled centres" % sample))
         try:
-            cb = cpu_reference(w, at, path, 1, 0, sample)
+            kept = {}
+            cb = cpu_reference(w, at, path, 1, 0, sample, keep=kept)
             cpu = {k: cb[k] for k in CPU_KEYS if k in cb}
             cpu["cpu_model"] = cpu_model()
-            from oracle import oracle
-            mask = sample_mask(n, sample) if sample else None
-            o = oracle.OracleModel.from_xml(path).calc(at.positions, at.numbers, at.lattice, [1, 1, 1], mask=mask,
-                                                       nthreads=os.cpu_count())
+            o, mask = kept["result"], kept["mask"]
             nc = sample or n
             errs = {}
             for prec, p in form_pots.items():
