@@ -469,7 +469,6 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     int* lst = spc + TC;                              // NS * TC
     int* lcnt = lst + NS * TC;                        // NS
     unsigned char* lofm = reinterpret_cast<unsigned char*>(lcnt + NS);  // L2
-    unsigned short* ptab = reinterpret_cast<unsigned short*>(lofm + ((L2 + 1) & ~1));  // n_pairs: ia << 8 | jb
     const int tid = threadIdx.x, bd = blockDim.x;
     copy_to_smem<4>(tab, K, tb.size);
     for (int k = tid; k < L2; k += bd) lofm[k] = (unsigned char)l_of_lm(k);
@@ -582,31 +581,45 @@ __global__ void __launch_bounds__(FWD_THREADS) k_soap_forward(SoapConst sc, cons
     __syncthreads();
     R* cg = c_out + (size_t)ci * sc.ncomp;
     for (int k = tid; k < sc.ncomp; k += bd) cg[k] = cs[k];
-    // power spectrum: one item per (l, pair); pairs decoded once into a table
+    // power spectrum: one item per (l, 2x2 block of channel rows (ia, jb), ia >= jb), so
+    // that each pair of loaded coefficients feeds two products
     R* ps = Ysm;
     R ssr = 0;
-    for (int pr = tid; pr < sc.n_pairs; pr += bd) {
-        int ia, jb;
-        decode_pair(pr, ia, jb);
-        ptab[pr] = (unsigned short)(ia << 8 | jb);
-    }
-    __syncthreads();
-    if (tid < sc.n_pairs * L) {
-        Walk2 w(tid, bd, sc.n_pairs);
-        for (; w.i < L; w.next()) {
-            const int l = w.i, pr = w.j, ia = ptab[pr] >> 8, jb = ptab[pr] & 255;
-            const R* ca = cs + ia * L2 + l * l;
-            const R* cb = cs + jb * L2 + l * l;
-            R v0 = 0, v1 = 0;
-            int m = 0;
-            for (; m + 1 < 2 * l + 1; m += 2) {
-                v0 += ca[m] * cb[m];
-                v1 += ca[m + 1] * cb[m + 1];
+    {
+        const int NR = NS * nm, NB = (NR + 1) / 2, nblk = NB * (NB + 1) / 2;
+        if (tid < nblk * L) {
+            Walk2 w(tid, bd, nblk);
+            for (; w.i < L; w.next()) {
+                const int l = w.i;
+                int bi = (int)((sqrtf((float)(8 * w.j + 1)) - 1.0f) * 0.5f);
+                while ((bi + 1) * (bi + 2) / 2 <= w.j) ++bi;
+                while (bi * (bi + 1) / 2 > w.j) --bi;
+                const int bj = w.j - bi * (bi + 1) / 2;
+                const int i0 = 2 * bi, j0 = 2 * bj;
+                const bool i1ok = i0 + 1 < NR, j1ok = j0 + 1 < NR;
+                const R* a0 = cs + i0 * L2 + l * l;
+                const R* a1 = cs + (i1ok ? i0 + 1 : i0) * L2 + l * l;
+                const R* b0 = cs + j0 * L2 + l * l;
+                const R* b1 = cs + (j1ok ? j0 + 1 : j0) * L2 + l * l;
+                R v00 = 0, v01 = 0, v10 = 0, v11 = 0;
+                for (int m = 0; m < 2 * l + 1; ++m) {
+                    const R x0 = a0[m], x1 = a1[m], y0 = b0[m], y1 = b1[m];
+                    v00 += x0 * y0;
+                    v01 += x0 * y1;
+                    v10 += x1 * y0;
+                    v11 += x1 * y1;
+                }
+                const R lf = K[tb.lf + l], r2 = (R)1.41421356237309504880;
+                auto put = [&](int ia, int jb, R v) {
+                    v *= (ia != jb ? r2 : (R)1) * lf;
+                    ps[(ia * (ia + 1) / 2 + jb) * L + l] = v;
+                    ssr += v * v;
+                };
+                put(i0, j0, v00);
+                if (j1ok && bi != bj) put(i0, j0 + 1, v01);
+                if (i1ok) put(i0 + 1, j0, v10);
+                if (i1ok && j1ok) put(i0 + 1, j0 + 1, v11);
             }
-            if (m < 2 * l + 1) v0 += ca[m] * cb[m];
-            const R v = (v0 + v1) * (ia != jb ? (R)1.41421356237309504880 : (R)1) * K[tb.lf + l];
-            ps[pr * L + l] = v;
-            ssr += v * v;
         }
     }
     // FP32 partial sums per warp, combined in FP64
