@@ -580,7 +580,10 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     if (warp == 0 && lane == 0) {
         // ---------------- TMA producer (both CTAs)
-        const uint64_t pol_a = policy_evict_first(), pol_b = policy_evict_last();
+        // L2 policy by tile order: in bands (group > 1) a row block of A is reused by every
+        // column block of its band, so it is kept like B; in the column-fastest order it is
+        // used only while its tiles are in flight
+        const uint64_t pol_a = group > 1 ? policy_evict_last() : policy_evict_first(), pol_b = policy_evict_last();
         int it = 0;
         bool ok = true;
         for (int tile = pair; tile < ntiles && ok; tile += npairs) {
