@@ -67,7 +67,9 @@ const char* gapgpu_last_error(void);
  * (src/Potentials/IPModel_GAP.f95:149-192): `label` selects the GAP_params stanza
  * (NULL/"" = first), sparseX_filename entries are resolved relative to `base_dir`
  * (the reference changes into the XML file's directory, Potential.f95:455-466).
- * `init_args` is the reference's init args_str (keys: label, E_scale). */
+ * `init_args` is the reference's init args_str (keys: label, E_scale, and
+ * gap_variance_regularisation, which sets up the variance estimate of every coordinate as
+ * IPModel_GAP.f95:170-187 does: K_MM + regularisation * I factorised once, in FP64). */
 int gapgpu_model_create(const char* xml, size_t xml_len, const char* init_args, const char* base_dir,
                         gapgpu_model** out);
 
@@ -91,8 +93,11 @@ void gapgpu_context_destroy(gapgpu_context* ctx);
  * is the logical property named by args_str atom_mask_name: it restricts the
  * centres (and the e0 sum) exactly as the reference does.  Recognised args keys:
  * atom_mask_name (value ignored here: pass the mask array), r_scale / E_scale
- * (rejected, as in IPModel_GAP.f95:348-350), xml_version, precision=fp64|bf16x3|tf32|fp16.
- * Unknown keys are ignored, like param_read_line(ignore_unknown=.true.). */
+ * (rejected, as in IPModel_GAP.f95:348-350), xml_version, precision=fp64|bf16x3|tf32|fp16,
+ * local_gap_variance=<name> / print_gap_variance=T (the variance estimate, read back with
+ * gapgpu_gap_variance / gapgpu_gap_variance_instances; needs gap_variance_regularisation in
+ * the model's init args).  Unknown keys are ignored, like
+ * param_read_line(ignore_unknown=.true.). */
 int gapgpu_calc(gapgpu_context* ctx, int n, const double* pos, const int32_t* Z, const double* lattice,
                 const int32_t* pbc, const int32_t* atom_mask, double* energy, double* local_e, double* force,
                 double* virial, double* local_virial, const char* args);
@@ -142,6 +147,24 @@ int gapgpu_context_set_option(gapgpu_context* ctx, const char* key, int value);
  * evaluation did not request the sums.  The calc argument only_descriptor=<k> (:334,
  * :399-403) evaluates only coordinate k (1-based) of a model with more than one. */
 int gapgpu_energy_per_coordinate(gapgpu_context* ctx, double* out, int capacity, int* count);
+
+/* GAP variance estimate of the last gapgpu_calc whose args requested it
+ * (local_gap_variance / print_gap_variance, IPModel_GAP.f95:330-335, :464-488):
+ * local_variance[n] = sum over descriptor instances containing the atom of
+ * sigma^2 fc^2 / |ci|, and variance_gradient[3n] (Fortran (3,N) layout) the property
+ * gap_variance_gradient, the derivative of the summed local variances with respect to each
+ * atom's position (available when that calculation computed forces or virials).
+ * sigma^2 = k(x,x) - k^T (K_MM + lambda I)^-1 k is the sparse-GP predictive variance, in
+ * FP64 whatever the context's precision.  Either output may be NULL. */
+int gapgpu_gap_variance(gapgpu_context* ctx, double* local_variance, double* variance_gradient, int n);
+
+/* The variance of every descriptor instance of coordinate `coordinate` (0-based) of that
+ * calculation -- what print_gap_variance prints (IPModel_GAP.f95:506-516): sigma^2, the
+ * squared covariance cutoff fc^2, and the instance's atoms (the centre and -1 for SOAP;
+ * i and j of the directed pair i -> j for distance_2b).  Writes at most capacity entries
+ * (NULL arrays skipped); *count receives the number of instances. */
+int gapgpu_gap_variance_instances(gapgpu_context* ctx, int coordinate, double* variance, double* fc2, int32_t* atom_i,
+                                  int32_t* atom_j, int capacity, int* count);
 
 /* Text report of the autotuner's choices so far (one line per GEMM shape: chosen N tile
  * and the time of every candidate).  Returns the report length; writes at most

@@ -36,6 +36,14 @@
 //   assembly    -- src/Potentials/IPModel_GAP.f95:233-605 (local energy split over ci,
 //                  f_gp = gradPredict.grad_data*fc + e*grad_fc, F(j) -= f_gp,
 //                  virial(j) -= (pos_n - pos_centre) (x) f_gp, e0, E_scale).
+//   variance    -- GAP gpCoordinates_initialise_variance_estimate / gp_predict's variance
+//                  (absent submodule; set up at IPModel_GAP.f95:185-187 from the init arg
+//                  gap_variance_regularisation, accumulated at :464-488).  Restated from the
+//                  published sparse-GP predictive variance sigma^2(x) = k(x,x) - k^T C^-1 k
+//                  with C = K_MM + lambda I (lambda = gap_variance_regularisation), k_s =
+//                  k(x, x_s) the covariance without alpha or sparseCutoff; its gradient is
+//                  grad k(x,x) - 2 (grad k)^T C^-1 k.  No fixture pins it (parity unpinned);
+//                  the tests check its gradient against finite differences.
 //
 // Build: oracle/Makefile -> oracle/_build/liboracle.so (g++ -O2 -ffp-contract=off -fopenmp).
 
@@ -550,6 +558,7 @@ struct Coordinate {
     std::vector<double> theta;
     int M = 0, D = 0;
     std::vector<double> X, alpha, sc;  // X[s*D + d]
+    std::vector<double> Lvar;          // Cholesky factor of K_MM + lambda I (lower, row-major), variance only
     double cutoff() const { return desc_type == DESC_SOAP ? soap.rc : d2_rc; }
 };
 
@@ -585,6 +594,89 @@ double gp_predict(const Coordinate& c, const double* x, double* gp) {
         }
     }
     return e;
+}
+
+// Covariance of two descriptor vectors, without alpha or sparseCutoff.
+double cov_pair(const Coordinate& c, const double* x, const double* y) {
+    const double d2 = c.delta * c.delta;
+    if (c.cov == COV_DOT_PRODUCT) {
+        double dot = 0;
+        for (int d = 0; d < c.D; ++d) dot += x[d] * y[d];
+        return d2 * std::pow(dot, c.zeta);
+    }
+    double ss = 0;
+    for (int d = 0; d < c.D; ++d) {
+        const double t = (x[d] - y[d]) / c.theta[d];
+        ss += t * t;
+    }
+    return d2 * std::exp(-0.5 * ss);
+}
+
+// C = K_MM + reg I and its Cholesky factor L (C = L L^T).  Returns -1 if C is not
+// positive definite.
+int init_variance(Coordinate& c, double reg) {
+    const int M = c.M;
+    std::vector<double>& L = c.Lvar;
+    L.assign((size_t)M * M, 0.0);
+    for (int s = 0; s < M; ++s)
+        for (int t = 0; t <= s; ++t) L[(size_t)s * M + t] = cov_pair(c, &c.X[(size_t)s * c.D], &c.X[(size_t)t * c.D]) +
+                                                            (s == t ? reg : 0.0);
+    for (int j = 0; j < M; ++j) {
+        double dj = L[(size_t)j * M + j];
+        for (int k = 0; k < j; ++k) dj -= L[(size_t)j * M + k] * L[(size_t)j * M + k];
+        if (!(dj > 0)) { L.clear(); return -1; }
+        dj = std::sqrt(dj);
+        L[(size_t)j * M + j] = dj;
+        for (int i = j + 1; i < M; ++i) {
+            double v = L[(size_t)i * M + j];
+            for (int k = 0; k < j; ++k) v -= L[(size_t)i * M + k] * L[(size_t)j * M + k];
+            L[(size_t)i * M + j] = v / dj;
+        }
+    }
+    return 0;
+}
+
+// sigma^2(x) = k(x,x) - k^T C^-1 k and, when grad is given, its gradient (D values).
+double gp_variance(const Coordinate& c, const double* x, double* grad) {
+    const int M = c.M, D = c.D;
+    const std::vector<double>& L = c.Lvar;
+    std::vector<double> k(M), y(M);
+    for (int s = 0; s < M; ++s) k[s] = cov_pair(c, x, &c.X[(size_t)s * D]);
+    for (int i = 0; i < M; ++i) {  // L z = k
+        double v = k[i];
+        for (int j = 0; j < i; ++j) v -= L[(size_t)i * M + j] * y[j];
+        y[i] = v / L[(size_t)i * M + i];
+    }
+    for (int i = M - 1; i >= 0; --i) {  // L^T y = z
+        double v = y[i];
+        for (int j = i + 1; j < M; ++j) v -= L[(size_t)j * M + i] * y[j];
+        y[i] = v / L[(size_t)i * M + i];
+    }
+    double var = cov_pair(c, x, x);
+    for (int s = 0; s < M; ++s) var -= k[s] * y[s];
+    if (grad) {
+        const double d2 = c.delta * c.delta;
+        std::fill(grad, grad + D, 0.0);
+        if (c.cov == COV_DOT_PRODUCT) {
+            double xx = 0;
+            for (int d = 0; d < D; ++d) xx += x[d] * x[d];
+            const double gxx = d2 * c.zeta * std::pow(xx, c.zeta - 1.0) * 2.0;
+            for (int d = 0; d < D; ++d) grad[d] = gxx * x[d];
+            for (int s = 0; s < M; ++s) {
+                const double* xs = &c.X[(size_t)s * D];
+                double dot = 0;
+                for (int d = 0; d < D; ++d) dot += x[d] * xs[d];
+                const double w = -2.0 * y[s] * d2 * c.zeta * std::pow(dot, c.zeta - 1.0);
+                for (int d = 0; d < D; ++d) grad[d] += w * xs[d];
+            }
+        } else {
+            for (int s = 0; s < M; ++s) {
+                const double* xs = &c.X[(size_t)s * D];
+                for (int d = 0; d < D; ++d) grad[d] += -2.0 * y[s] * k[s] * (xs[d] - x[d]) / (c.theta[d] * c.theta[d]);
+            }
+        }
+    }
+    return var;
 }
 
 struct Instance {
@@ -863,5 +955,75 @@ int oracle_gap_calc(void* mp, int n, const double* pos, const int* Z, const doub
 }
 
 int oracle_model_n_coordinates(void* mp) { return (int)static_cast<Model*>(mp)->coords.size(); }
+
+// Variance estimate set-up for every coordinate (the init arg gap_variance_regularisation,
+// IPModel_GAP.f95:185-187).  Returns -1 if some K_MM + reg I is not positive definite.
+int oracle_model_init_variance(void* mp, double reg) {
+    for (Coordinate& c : static_cast<Model*>(mp)->coords)
+        if (init_variance(c, reg) != 0) return -1;
+    return 0;
+}
+
+// The calc arguments local_gap_variance / print_gap_variance (IPModel_GAP.f95:330-335,
+// 464-488, 506-516): per atom local_var[a] = sum over instances with a in ci of
+// sigma^2 fc^2 / |ci|, and (var_grad, 3*n, may be NULL) gap_variance_gradient(:,j) = sum
+// over gradient entries n = j of grad sigma^2 . grad_data(:,:,n) fc^2 + 2 sigma^2 fc
+// grad_fc(:,n).  inst_var (may be NULL, capacity inst_cap): sigma^2 of every instance, in
+// instance order, coordinate after coordinate; returns the number of instances, or -1.
+long oracle_gap_variance(void* mp, int n, const double* pos, const int* Z, const double* lattice, const int* pbc,
+                         const int* mask, int select, int only, double* local_var, double* var_grad, double* inst_var,
+                         long inst_cap, int nthreads) {
+    Model& m = *static_cast<Model*>(mp);
+    NeighbourList nl;
+    if (build_neighbours(n, pos, lattice, pbc, model_cutoff(m), nl) != 0) return -1;
+    for (const Coordinate& c : m.coords)
+        if (c.Lvar.empty()) return -1;
+    const bool do_grad = var_grad != nullptr;
+    std::vector<double> lv(n, 0.0), g(3 * (size_t)n, 0.0);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    long ninst = 0;
+    const int ncoord = (int)m.coords.size();
+    for (int kc = 0; kc < ncoord; ++kc) {
+        const Coordinate& c = m.coords[kc];
+        if (select && ncoord > 1 && kc + 1 != only) continue;
+        std::vector<std::pair<int, int>> inst;
+        enumerate_instances(c, n, Z, pos, nl, mask, inst);
+        const long ni = (long)inst.size();
+        std::vector<double> var_k(ni, 0.0);
+#pragma omp parallel
+        {
+            std::vector<double> lv_t(n, 0.0), g_t(3 * (size_t)n, 0.0), gv(c.D);
+            Instance I;
+#pragma omp for schedule(dynamic)
+            for (long k = 0; k < ni; ++k) {
+                make_instance(c, inst[k].first, inst[k].second, Z, pos, nl, do_grad, I);
+                const double v = gp_variance(c, I.x.data(), do_grad ? gv.data() : nullptr);
+                var_k[k] = v;
+                for (int a : I.ci) lv_t[a] += v * I.fc * I.fc / (double)I.ci.size();
+                if (!do_grad) continue;
+                for (size_t en = 0; en < I.ii.size(); ++en) {
+                    for (int q3 = 0; q3 < 3; ++q3) {
+                        const double* gd = &I.grad[(en * 3 + q3) * c.D];
+                        double t = 0;
+                        for (int d = 0; d < c.D; ++d) t += gv[d] * gd[d];
+                        g_t[3 * (size_t)I.ii[en] + q3] += t * I.fc * I.fc + 2.0 * v * I.fc * I.gfc[3 * en + q3];
+                    }
+                }
+            }
+#pragma omp critical
+            {
+                for (int a = 0; a < n; ++a) lv[a] += lv_t[a];
+                for (size_t a = 0; a < g.size(); ++a) g[a] += g_t[a];
+            }
+        }
+        for (long k = 0; k < ni; ++k, ++ninst)
+            if (inst_var && ninst < inst_cap) inst_var[ninst] = var_k[k];
+    }
+    if (local_var) std::memcpy(local_var, lv.data(), sizeof(double) * n);
+    if (var_grad) std::memcpy(var_grad, g.data(), sizeof(double) * 3 * n);
+    return ninst;
+}
 
 }  // extern "C"

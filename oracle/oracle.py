@@ -59,6 +59,10 @@ def lib():
         L.oracle_gap_calc_ex.argtypes = [v, i, P(d), P(i), P(d), P(i), P(i), i, i, P(d), P(d), P(d), P(d), P(d), P(d), i]
         L.oracle_model_n_coordinates.restype = i
         L.oracle_model_n_coordinates.argtypes = [v]
+        L.oracle_model_init_variance.restype = i
+        L.oracle_model_init_variance.argtypes = [v, d]
+        L.oracle_gap_variance.restype = l
+        L.oracle_gap_variance.argtypes = [v, i, P(d), P(i), P(d), P(i), P(i), i, i, P(d), P(d), P(d), l, i]
         _lib = L
     return _lib
 
@@ -248,6 +252,34 @@ class OracleModel:
             lib().oracle_model_free(self._h)
         except Exception:
             pass
+
+    def init_variance(self, regularisation=0.001):
+        """Variance estimate set-up, as the init arg gap_variance_regularisation
+        (IPModel_GAP.f95:185-187): K_MM + regularisation * I factorised per coordinate."""
+        if lib().oracle_model_init_variance(self._h, float(regularisation)) != 0:
+            raise ValueError("K_MM + regularisation I is not positive definite")
+
+    def variance(self, pos, Z, lattice, pbc=(1, 1, 1), mask=None, gradient=True, nthreads=0, only_descriptor=None):
+        """local_gap_variance (N,), gap_variance_gradient (N,3) and the variance of every
+        descriptor instance (IPModel_GAP.f95:464-488, 506-516)."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        n = len(pos)
+        Z = np.ascontiguousarray(Z, dtype=np.int32)
+        lat = np.asfortranarray(lattice, dtype=np.float64).ravel(order="F").copy()
+        pbc = np.ascontiguousarray(np.asarray(pbc, dtype=np.int32).reshape(3))
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        lv = np.zeros(n)
+        g = np.zeros((n, 3)) if gradient else None
+        sel = only_descriptor is not None
+        L = lib()
+        args = (self._h, n, _dp(pos), _ip(Z), _dp(lat), _ip(pbc), _ip(m), int(sel), int(only_descriptor) if sel else 0,
+                _dp(lv), _dp(g))
+        ni = L.oracle_gap_variance(*args, None, 0, nthreads)
+        if ni < 0:
+            raise RuntimeError("oracle_gap_variance failed (variance not initialised?)")
+        iv = np.zeros(ni)
+        L.oracle_gap_variance(*args, _dp(iv), ni, nthreads)
+        return dict(local_gap_variance=lv, gap_variance_gradient=g, instance_variance=iv)
 
     def calc(self, pos, Z, lattice, pbc=(1, 1, 1), mask=None, nthreads=0, only_descriptor=None):
         """E, local_e, F (N,3), virial (3,3), local_virial (N,3,3) and energy_per_coordinate

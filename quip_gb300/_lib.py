@@ -22,7 +22,8 @@ EXPORTS = ["gapgpu_last_error", "gapgpu_model_create", "gapgpu_model_cutoff", "g
            "gapgpu_context_set_option", "gapgpu_model_footprint", "gapgpu_md_create", "gapgpu_md_step", "gapgpu_md_state",
            "gapgpu_md_counters", "gapgpu_md_context", "gapgpu_md_destroy", "gapgpu_tuning_report",
            "gapgpu_selftest_bounded_wait", "gapgpu_calc_lammps", "gapgpu_energy_per_coordinate",
-           "gapgpu_probe_fp32_rate", "gapgpu_context_neighbours"]
+           "gapgpu_probe_fp32_rate", "gapgpu_context_neighbours", "gapgpu_gap_variance",
+           "gapgpu_gap_variance_instances"]
 
 
 class GapGpuError(RuntimeError):
@@ -88,6 +89,8 @@ def load(build_if_missing=True):
     L.gapgpu_context_timings.argtypes = [c_void_p, P(c_double), c_int]
     L.gapgpu_context_launches.argtypes = [c_void_p, P(i64)]
     L.gapgpu_probe_fp32_rate.argtypes = [c_void_p, P(c_double)]
+    L.gapgpu_gap_variance.argtypes = [c_void_p, c_void_p, c_void_p, c_int]
+    L.gapgpu_gap_variance_instances.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, P(c_int)]
     L.gapgpu_context_neighbours.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, i64, P(i64)]
     L.gapgpu_energy_per_coordinate.argtypes = [c_void_p, c_void_p, c_int, P(c_int)]
     _lib = L

@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgapgpu.so")
-SOURCES = ["model.cpp", "neighbours.cu", "soap.cu", "gp64.cu", "tcgen05.cu", "pair.cu", "calc.cu", "md.cu"]
+SOURCES = ["model.cpp", "neighbours.cu", "soap.cu", "gp64.cu", "tcgen05.cu", "pair.cu", "calc.cu", "md.cu", "variance.cu"]
+LIBS = ["-lcublas", "-lcusolver"]  # the variance estimate's FP64 GEMMs and Cholesky factor
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-Xcompiler", "-Wall"]
 
@@ -48,7 +49,7 @@ def build(verbose=False, extra=()):
         objs = list(ex.map(lambda s: _compile(s, list(extra)), SOURCES))
     if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs):
         return LIB
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + LIBS
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

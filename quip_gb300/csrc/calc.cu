@@ -25,6 +25,7 @@ struct ArgOpts {
     int precision = -1;
     bool bad_scale = false;
     bool select = false, epc = false;  // only_descriptor given; energy_per_coordinate requested
+    bool var = false;                   // local_gap_variance / print_gap_variance requested
     int only = 0;
 };
 
@@ -44,10 +45,14 @@ int parse_calc_args(const char* args, ArgOpts& o) {
         else if (p == "fp16") o.precision = GAPGPU_MIXED_F16;
         else GG_FAIL(GAPGPU_ERR_ARG, "precision must be fp64, bf16x3, tf32 or fp16");
     }
-    for (const char* k : {"local_gap_variance", "print_gap_variance"}) {
-        auto it = a.find(k);
-        if (it != a.end() && it->second != "" && it->second != "F" && it->second != "0")
-            GG_FAIL(GAPGPU_ERR_UNSUPPORTED, std::string("calc option ") + k + " is not supported by this library");
+    // local_gap_variance=<name> (a non-empty name) and print_gap_variance=T request the
+    // variance estimate (IPModel_GAP.f95:330-335, :362-364)
+    {
+        auto lv = a.find("local_gap_variance");
+        auto pv = a.find("print_gap_variance");
+        const bool print = pv != a.end() && (pv->second == "" || pv->second == "T" || pv->second == "t" ||
+                                              pv->second == "true" || pv->second == "True" || pv->second == "1");
+        o.var = (lv != a.end() && !lv->second.empty()) || print;
     }
     // only_descriptor (IPModel_GAP.f95:334, :399-403): given at all, it selects the coordinate
     // of that 1-based index when the model has more than one
@@ -92,6 +97,8 @@ void apply_call_opts(gapgpu_context& c, const ArgOpts& o) {
     c.only_coord = o.only;
     c.want_epc = o.epc;
     c.epc_valid = false;
+    c.want_var = o.var;
+    c.var_valid = false;
 }
 
 int check_device() {
@@ -153,8 +160,9 @@ void free_model_device(gapgpu_model& m) {
     for (Coordinate& co : m.coords) {
         for (void* p : {(void*)co.dX64, (void*)co.dcoef, (void*)co.dXf32, (void*)co.dXhi, (void*)co.dXlo, (void*)co.dXTf32,
                         (void*)co.dXThi, (void*)co.dXTlo, (void*)co.dXTh16, (void*)co.dXh16, (void*)co.dcoef32,
-                        (void*)co.dtheta, co.dtab[0], co.dtab[1]})
+                        (void*)co.dtheta, (void*)co.dVarL, co.dtab[0], co.dtab[1]})
             if (p) cudaFree(p);
+        co.dVarL = nullptr;
         co.dtab[0] = co.dtab[1] = nullptr;
         co.dXTh16 = nullptr;
         co.dXh16 = nullptr;
@@ -432,6 +440,7 @@ gapgpu_context::~gapgpu_context() {
     for (cudaEvent_t e : cev)
         if (e) cudaEventDestroy(e);
     if (graph) cudaGraphExecDestroy(graph);
+    destroy_handles(*this);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -501,6 +510,7 @@ int gapgpu_model_create(const char* xml, size_t xml_len, const char* init_args, 
     int rc = parse_model(xml, xml_len ? xml_len : (xml ? std::strlen(xml) : 0), init_args, base_dir, *m);
     if (!rc) rc = upload_model(*m);
     if (!rc) rc = prepare_mixed_operands(*m);
+    if (!rc && m->var_requested) rc = variance_setup(*m, m->var_reg);
     if (rc) {
         free_model_device(*m);
         delete m;
@@ -645,11 +655,21 @@ int gapgpu_calc(gapgpu_context* c, int n, const double* pos, const int32_t* Z, c
         if (virial) std::memset(virial, 0, 9 * sizeof(double));
         return GAPGPU_OK;
     }
+    if (o.var && !c->model->var_ready)
+        GG_FAIL(GAPGPU_ERR_ARG,
+                "local_gap_variance / print_gap_variance need the init argument gap_variance_regularisation");
     if ((rc = copy_inputs(*c, n, pos, Z, atom_mask, cudaMemcpyHostToDevice))) return rc;
     const int* dmask = atom_mask ? c->mask.as<int>() : nullptr;
     if ((rc = prepare(*c, 1, &n, lattice, pbc, dmask, c->model->cutoff, LIST_BUILD, prec))) return rc;
     if ((rc = run_evaluation(*c, prec, dmask))) return rc;
     c->epc_valid = c->want_epc;
+    if (o.var) {
+        const int saved = c->precision;
+        c->precision = prec;
+        rc = variance_eval(*c, dmask, force || virial || local_virial);
+        c->precision = saved;
+        if (rc) return rc;
+    }
     double red[10];
     GG_CUDA(cudaMemcpyAsync(red, c->out_e.p, sizeof red, cudaMemcpyDeviceToHost, c->stream));
     if (force) GG_CUDA(cudaMemcpyAsync(force, c->out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
@@ -687,6 +707,7 @@ int gapgpu_calc_batch(gapgpu_context* c, int nstruct, const int32_t* n_atoms, co
     ArgOpts o;
     int rc;
     if ((rc = parse_calc_args(args, o))) return rc;
+    if (o.var) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "the GAP variance is computed by gapgpu_calc (one structure per call)");
     apply_call_opts(*c, o);
     const CallPrecision cp(*c, o.precision);
     const int prec = cp.prec;

@@ -75,6 +75,13 @@ struct gapgpu_context {
     bool sel_coord = false, want_epc = false, epc_valid = false;
     int only_coord = 0;
     gapgpu::DBuf epc_out, epca, epcp;         // [nstruct x ncoord]; per-atom and per-pair scratch
+    // GAP variance of the last gapgpu_calc that requested it (local_gap_variance / print_gap_variance):
+    // per-atom variances, minus their gradients, scratch, instance variances per coordinate
+    bool want_var = false, var_valid = false, var_has_grad = false;
+    gapgpu::DBuf var_le, var_f, var_lv, var_zero, var_info, var_q, var_k, var_y, var_g, var_inst;
+    std::vector<long long> var_inst_off;
+    void* blas = nullptr;                     // cuBLAS and cuSOLVER handles of the variance pass
+    void* solver = nullptr;
     std::vector<int> h_chunks, h_schunk;
     int nstruct = 0, n_total = 0;
     // CUDA graph of the evaluation phase, keyed by shapes and buffer addresses
@@ -100,7 +107,8 @@ struct gapgpu_context {
                 &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev,
                 &nbr_i, &wpos, &total, &geoms, &sid, &dispmax, &phi, &plo, &fpair, &epair, &eatom, &redpart, &flags, &centres,
                 &ncent, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf, &Wlo, &epart, &ecent, &Gbuf, &scratch, &chunks, &schunk,
-                &epc_out, &epca, &epcp};
+                &epc_out, &epca, &epcp, &var_le, &var_f, &var_lv, &var_zero, &var_info, &var_q, &var_k, &var_y,
+                &var_g, &var_inst};
     }
     std::vector<const gapgpu::DBuf*> buffers() const {
         std::vector<gapgpu::DBuf*> b = const_cast<gapgpu_context*>(this)->buffers();
@@ -144,4 +152,10 @@ bool coordinate_chosen(const gapgpu_context& c, int k);
 // the descriptors in FP16) when the model's FP16 operands exist
 bool gemm1_f16_active(const gapgpu_context& c, const Coordinate& co);
 int gather_outputs(gapgpu_context& c, const gapgpu_model& m, int n, const int* d_mask);
+// the per-atom gather of fpair / epair / eatom into given outputs (no mask, e0 per Z given)
+int gather_into(gapgpu_context& c, int n, const double* e0, double escale, double* le, double* F, double* LV);
+// variance.cu: GAP variance estimate (set-up per model, pass after an evaluation)
+int variance_setup(gapgpu_model& m, double reg);
+int variance_eval(gapgpu_context& c, const int* d_mask, bool grad);
+void destroy_handles(gapgpu_context& c);
 }  // namespace gapgpu

@@ -88,6 +88,7 @@ struct Coordinate {
     uint16_t* dXTlo = nullptr;
     float* dcoef32 = nullptr;
     double* dtheta = nullptr;   // distance_2b
+    double* dVarL = nullptr;    // [M][M] Cholesky factor of K_MM + lambda I (column-major lower), variance only
     void* dtab[2] = {nullptr, nullptr};  // SOAP constant block (soap_tab layout): [0] FP64, [1] FP32
 };
 
@@ -101,6 +102,8 @@ struct gapgpu_model {
     std::string label;
     int xml_version = 0;
     int device = 0;
+    bool var_requested = false, var_ready = false;  // init arg gap_variance_regularisation given / set up
+    double var_reg = 0.001;
     double* de0 = nullptr;  // e0 per Z on the device
 };
 

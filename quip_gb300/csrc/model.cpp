@@ -350,6 +350,13 @@ int parse_model(const char* xml, size_t len, const char* init_args, const char* 
     std::map<std::string, std::string> ia = parse_args(init_args ? init_args : "");
     std::string label = ia.count("label") ? ia["label"] : "";
     if (ia.count("E_scale")) to_double(ia["E_scale"], m.E_scale);
+    // the variance estimate is set up only when the init args name its regularisation
+    // (IPModel_GAP.f95:170-171, :185-187)
+    if (ia.count("gap_variance_regularisation")) {
+        m.var_requested = true;
+        if (!to_double(ia["gap_variance_regularisation"], m.var_reg) || !(m.var_reg >= 0))
+            GG_FAIL(GAPGPU_ERR_ARG, "gap_variance_regularisation must be a non-negative number");
+    }
     XParser p(xml, len);
     std::unique_ptr<XNode> root = p.element();
     if (!root) GG_FAIL(GAPGPU_ERR_XML, "GAP XML parse error: " + p.err);

@@ -348,6 +348,16 @@ int pair_2b(gapgpu_context& c, const std::vector<const Coordinate*>& coords, con
     return GAPGPU_OK;
 }
 
+int gather_into(gapgpu_context& c, int n, const double* e0, double escale, double* le, double* F, double* LV) {
+    const int TB = 128;
+    k_gather<<<(n + TB - 1) / TB, TB, 0, c.stream>>>(n, c.Z.as<int>(), nullptr, c.nbr_off.as<int>(), c.nbr_rev.as<int>(),
+                                                    c.nbr_d.as<double4>(), c.fpair.as<double>(), c.epair.as<double>(),
+                                                    c.eatom.as<double>(), e0, escale, le, F, LV);
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
 int gather_outputs(gapgpu_context& c, const gapgpu_model& m, int n, const int* d_mask) {
     const int nchunks = (int)c.h_chunks.size() / 2, ns = c.nstruct;
     const int TB = 128;

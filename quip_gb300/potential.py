@@ -21,6 +21,14 @@ def _epc_name(args_str):
     return m.group(1) if m else None
 
 
+def _variance_request(args_str):
+    """(name of local_gap_variance=<name> or None, print_gap_variance given true)."""
+    m = re.search(r"(?:^|\s)local_gap_variance=(\S+)", args_str or "")
+    p = re.search(r"(?:^|\s)print_gap_variance(?:=(\S+))?(?:\s|$)", args_str or "")
+    printed = bool(p) and (p.group(1) is None or p.group(1) in ("T", "t", "true", "True", "1"))
+    return (m.group(1) if m else None), printed
+
+
 def _init_args_from_xml(xml):
     """Default init args from the first <Potential init_args=...> tag (Potential.f95:525-538)."""
     m = re.search(r'<Potential[^>]*init_args="([^"]*)"', xml)
@@ -141,7 +149,11 @@ class Potential:
         energy (float), force (N,3), virial (3,3), local_energy (N,), local_virial (N,3,3).
         ``atom_mask`` is the logical property that args_str atom_mask_name names.
         args_str "energy_per_coordinate=<name>" adds out[<name>] (one value per coordinate,
-        IPModel_GAP.f95:462,570); "only_descriptor=<k>" evaluates only coordinate k."""
+        IPModel_GAP.f95:462,570); "only_descriptor=<k>" evaluates only coordinate k;
+        "local_gap_variance=<name>" adds out[<name>] (per-atom variance estimate) and, with
+        forces, out["gap_variance_gradient"] (N,3); "print_gap_variance=T" prints every
+        descriptor instance's variance (IPModel_GAP.f95:464-488, 506-516).  The variance
+        needs gap_variance_regularisation in the potential's init args."""
         pos, Z, lat, pbc = self._arrays(at)
         n = len(pos)
         E = np.zeros(1)
@@ -167,8 +179,48 @@ class Potential:
         name = _epc_name(args_str)
         if name:
             out[name] = self._energy_per_coordinate(1)[0]
+        vname, vprint = _variance_request(args_str)
+        if vname or vprint:
+            grad = force or virial or local_virial
+            lv = np.zeros(n)
+            gv = np.zeros((n, 3)) if grad else None
+            _lib.check(self._L.gapgpu_gap_variance(self._ctx, _lib.ptr(lv), _lib.ptr(gv), n))
+            if vname:
+                out[vname] = lv
+                if grad:
+                    out["gap_variance_gradient"] = gv
+            if vprint:
+                self._print_gap_variance()
         self.results = out
         return out
+
+    def gap_variance_instances(self, coordinate):
+        """The variance of every descriptor instance of a coordinate (0-based) in the last
+        calc that requested the variance: dict variance, fc2, atom_i, atom_j."""
+        cnt = _lib.ctypes.c_int()
+        _lib.check(self._L.gapgpu_gap_variance_instances(self._ctx, coordinate, None, None, None, None, 0,
+                                                          _lib.ctypes.byref(cnt)))
+        k = cnt.value
+        v, f2 = np.zeros(k), np.zeros(k)
+        ai, aj = np.zeros(k, np.int32), np.zeros(k, np.int32)
+        _lib.check(self._L.gapgpu_gap_variance_instances(self._ctx, coordinate, _lib.ptr(v), _lib.ptr(f2), _lib.ptr(ai),
+                                                          _lib.ptr(aj), k, _lib.ctypes.byref(cnt)))
+        return dict(variance=v, fc2=f2, atom_i=ai, atom_j=aj)
+
+    def _print_gap_variance(self):
+        """print_gap_variance: one line per descriptor instance, as IPModel_GAP.f95:506-516
+        prints them (atoms 1-based)."""
+        label = re.search(r"label=(\S+)", self.args_str)
+        label = label.group(1) if label else ""
+        for k in range(self.n_coordinates()):
+            d = self.gap_variance_instances(k)
+            if len(d["variance"]) == 0:
+                print("GAP_VARIANCE potential %s descriptor %d not found" % (label, k + 1))
+            for i, (v, f2, a, b) in enumerate(zip(d["variance"], d["fc2"], d["atom_i"], d["atom_j"])):
+                print("GAP_VARIANCE potential %s descriptor %d var( %d ) = %.16g * %.16g cutoff" % (label, k + 1, i + 1, v,
+                                                                                                     f2))
+                print("GAP_VARIANCE potential %s descriptor %d ii( %d ) = %s" % (label, k + 1, i + 1,
+                                                                                " ".join(str(x + 1) for x in (a, b) if x >= 0)))
 
     def _energy_per_coordinate(self, nstruct):
         ncoord = self.n_coordinates()
