@@ -311,6 +311,7 @@ def measure_serving(path, precision, pool, loads, seconds, replicas=64, seed=11,
     log("serving: warm-up %.2f s" % warm)
     rng = np.random.default_rng(seed)
     out = {"precision": precision, "md_replicas": replicas, "md_atoms": int(md.n_atoms.sum()), "workers": 2,
+           "gemm_tiles": "single-CTA (the server's default: no CTA-pair tiles from concurrent streams)",
            "warmup_s": warm, "loads": []}
     for rate in loads:
         count = max(20, int(rate * seconds))

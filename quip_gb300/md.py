@@ -88,6 +88,10 @@ class MDReplicas:
     def set_stream(self, cuda_stream):
         _lib.check(self._L.gapgpu_context_set_stream(self.context(), _lib.ctypes.c_void_p(cuda_stream)))
 
+    def set_option(self, key, value):
+        """Options of the replicas' context (gapgpu_context_set_option), as Potential.set_option."""
+        _lib.check(self._L.gapgpu_context_set_option(self.context(), key.encode(), int(value)))
+
     def step(self, nsteps=1):
         _lib.check(self._L.gapgpu_md_step(self._md, int(nsteps)))
 

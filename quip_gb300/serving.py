@@ -56,16 +56,29 @@ def poisson_arrivals(rate, count, seed=0):
 
 
 class Server:
-    """Server(param_filename, precision="tf32", workers=2, budget_bytes=None, md=None)
+    """Server(param_filename, precision="tf32", workers=2, budget_bytes=None, md=None,
+    pair_tiles=False)
 
     ``md`` is an MDReplicas object whose replicas step alongside the requests (built on
-    its own Potential, so on its own context and stream)."""
+    its own Potential, so on its own context and stream).
 
-    def __init__(self, param_filename, precision="tf32", workers=2, budget_bytes=None, md=None, mean_neighbours=60.0):
+    ``pair_tiles=False`` (the default) runs every context the server drives, the
+    workers' and the MD replicas', on single-CTA GEMM tiles (context option pairs=0; the
+    fp16 form then computes its GEMMs in TF32).  With CTA-pair (cluster) GEMM tiles
+    issued from several streams at once -- two workers and the MD stream -- the device
+    stalled under load: a GEMM kernel stayed resident and never finished, at 1500-4000
+    requests/s.  Single-CTA tiles ran the same loads without a stall."""
+
+    def __init__(self, param_filename, precision="tf32", workers=2, budget_bytes=None, md=None, mean_neighbours=60.0,
+                 pair_tiles=False):
         self.pots = [Potential(param_filename=param_filename, precision=precision) for _ in range(max(1, workers))]
         for p in self.pots:
             p.set_option("timing", 0)
             p.set_option("priority", 1)   # requests ahead of the background MD stream
+            if not pair_tiles:
+                p.set_option("pairs", 0)
+        if md is not None and not pair_tiles:
+            md.set_option("pairs", 0)
         self.md = md
         self.mean_neighbours = mean_neighbours
         if budget_bytes is None:

@@ -187,6 +187,7 @@ def test_serving_results_are_the_same_alone_and_in_the_mix(sic_gap):
     assert stats["batches"] < len(structs)          # requests were batched together
     assert stats["p99_ms"] >= stats["p50_ms"] > 0
     alone = _pot(sic_gap, "tf32")
+    alone.set_option("pairs", 0)   # the server's contexts run single-CTA GEMM tiles
     for r in reqs:
         a = alone.calc(r.atoms)
         assert abs(a["energy"] - r.result["energy"]) <= 1e-12 * max(1.0, abs(a["energy"]))
