@@ -33,6 +33,7 @@ write) between timed steps.  `--impl reference` times the FP64 CPU restatement o
 reference (oracle/) on the host cores.  Progress goes to stderr with elapsed times.
 """
 import argparse
+import contextlib
 import json
 import os
 import signal
@@ -162,6 +163,74 @@ class Clocks:
             return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(rows)}
         except Exception as e:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "error": str(e)[:80]}
+
+
+class NvmlClocks:
+    """SM clock and clock-event reasons of this process's GPU read through NVML
+    (libnvidia-ml, the library nvidia-smi reads) every `period` seconds in a thread, so
+    that a timed region of a few tens of milliseconds still gets several samples.  Read
+    only: nothing is set."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, period=0.01):
+        import ctypes
+        import torch
+        self.ct, self.period = ctypes, period
+        self.L = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.L.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        props = torch.cuda.get_device_properties(torch.cuda.current_device())
+        rc = self.L.nvmlDeviceGetHandleByUUID(("GPU-%s" % props.uuid).encode(), ctypes.byref(self.h))
+        if rc != 0:
+            bus = "%08X:%02X:%02X.0" % (props.pci_domain_id, props.pci_bus_id, props.pci_device_id)
+            rc = self.L.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h))
+        if rc != 0:
+            raise RuntimeError("no NVML handle for this GPU (%d)" % rc)
+        self.reasons_fn = getattr(self.L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.L.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        self.L.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx))   # NVML_CLOCK_SM
+        self.max_mhz = float(mx.value)
+        self.samples = []
+
+    def _poll(self):
+        ct = self.ct
+        mhz, reasons = ct.c_uint(), ct.c_ulonglong()
+        while not self.stop.is_set():
+            if self.L.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.h, ct.byref(reasons)) == 0:
+                self.samples.append((float(mhz.value), int(reasons.value)))
+            self.stop.wait(self.period)
+
+    def __enter__(self):
+        import threading
+        self.stop = threading.Event()
+        self.t = threading.Thread(target=self._poll, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=5)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": [], "samples": 0, "source": "nvml"}
+        reasons = sorted({nm for _, r in self.samples for bit, nm in self.REASONS.items() if r & bit})
+        return {"sm_mhz": float(np.median([m for m, _ in self.samples])), "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(self.samples),
+                "source": "NVML every %g ms during the timed steps" % (1e3 * self.period)}
+
+
+def clock_sampler(path):
+    """NvmlClocks, else nvidia-smi every 200 ms (Clocks)."""
+    try:
+        return NvmlClocks()
+    except Exception as e:
+        log("clocks: NVML unavailable (%s), sampling with nvidia-smi" % str(e)[:80])
+        return Clocks(path)
 
 
 def cpu_model():
@@ -489,7 +558,7 @@ def main():
     d_pos = torch.tensor(at.positions, dtype=torch.float64, device="cuda").contiguous()
     d_Z = torch.tensor(at.numbers, dtype=torch.int32, device="cuda")
 
-    def device_run(pot, steps, warm):
+    def device_run(pot, steps, warm, timed_clocks=None):
         L = pot._L
         _lib.check(L.gapgpu_context_set_stream(pot._ctx, _lib.ctypes.c_void_p(stream.cuda_stream)))
         d_E = torch.zeros(1, dtype=torch.float64, device="cuda")
@@ -508,14 +577,15 @@ def main():
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         stage = np.zeros(len(STAGES))
         launches = 0
-        for k in range(steps):
-            flush.zero_()
-            evs[k][0].record(stream)
-            step()
-            evs[k][1].record(stream)
-            stage += np.array(list(pot.timings().values()))
-            launches += pot.launches()
-        torch.cuda.synchronize()
+        with timed_clocks if timed_clocks is not None else contextlib.nullcontext():
+            for k in range(steps):
+                flush.zero_()
+                evs[k][0].record(stream)
+                step()
+                evs[k][1].record(stream)
+                stage += np.array(list(pot.timings().values()))
+                launches += pot.launches()
+            torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
         ms = [a.elapsed_time(b) for a, b in evs]
@@ -531,10 +601,13 @@ def main():
     pot.set_option("pairs", args.gemm_pairs)
     if args.no_autotune:
         pot.set_option("autotune", 0)
-    clk = Clocks(os.path.join(tmp, "clocks.csv"))
-    with clk:
+    clk = clock_sampler(os.path.join(tmp, "clocks.csv"))
+    # NVML samples only the timed steps; nvidia-smi needs its start-up time, so it runs
+    # from before the warm-up
+    nvml = isinstance(clk, NvmlClocks)
+    with contextlib.nullcontext() if nvml else clk:
         t_wall0 = time.perf_counter()
-        run = device_run(pot, args.steps, warmup)
+        run = device_run(pot, args.steps, warmup, timed_clocks=clk if nvml else None)
         t_wall = time.perf_counter() - t_wall0
     t_dev = max_over_ranks(run["t"])
     value = world * n * args.steps / t_dev
