@@ -67,6 +67,7 @@ struct gapgpu_context {
     gapgpu::DBuf fpair, epair, eatom, redpart;
     // SOAP / GP workspace
     gapgpu::DBuf flags, centres, ncent, qbuf, qlo, pnorm, Kbuf, Wbuf, Wlo, epart, ecent, Gbuf, scratch;
+    gapgpu::DBuf hbuf, a2c;                   // FP32 SOAP backward: h per centre, atom -> centre
     int* cur_centres = nullptr;               // centre list of the coordinate being evaluated
     std::vector<int> nc_coord;                // centres per coordinate (prepare phase)
     gapgpu::DBuf chunks, schunk;              // segmented-reduction tables (per batch)
@@ -90,6 +91,7 @@ struct gapgpu_context {
     int graph_mode = 0;                       // 0: never, 1: capture on the second identical call
     bool autotune = true;                     // time the GEMM tile candidates of a new shape once
     int gemm_pairs = 1;                       // CTA-pair GEMM tiles: 0 off, 1 autotuner candidates, 2 only
+    int soap_bwd_nb = 1;                      // FP32 SOAP backward: 1 h kernel + one thread per pair where the basis allows, 0 one block per centre
     bool gemm2_f16 = false;                   // TF32 mode: FP16 second GEMM where the model allows it
     bool gemm1_f16 = false;                   // ... and FP16 first GEMM (on for GAPGPU_MIXED_F16 contexts)
     long long graph_hits = 0, graph_launches = 0;
@@ -107,7 +109,7 @@ struct gapgpu_context {
                 &cell_start, &cell_end, &ms, &cub_tmp, &minmax, &nbr_cnt, &nbr_off, &nbr_j, &nbr_d, &nbr_s, &nbr_rev,
                 &nbr_i, &wpos, &total, &geoms, &sid, &dispmax, &phi, &plo, &fpair, &epair, &eatom, &redpart, &flags, &centres,
                 &ncent, &qbuf, &qlo, &pnorm, &Kbuf, &Wbuf, &Wlo, &epart, &ecent, &Gbuf, &scratch, &chunks, &schunk,
-                &epc_out, &epca, &epcp, &var_le, &var_f, &var_lv, &var_zero, &var_info, &var_q, &var_k, &var_y,
+                &epc_out, &epca, &epcp, &hbuf, &a2c, &var_le, &var_f, &var_lv, &var_zero, &var_info, &var_q, &var_k, &var_y,
                 &var_g, &var_inst};
     }
     std::vector<const gapgpu::DBuf*> buffers() const {

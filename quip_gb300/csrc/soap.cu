@@ -25,6 +25,7 @@
 #include <cuda_fp16.h>
 #include <cmath>
 #include <vector>
+#include <mutex>
 #include "context.h"
 
 namespace gapgpu {
@@ -894,6 +895,315 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
     if (tid < 3 * prev_cnt) fpair[3 * (size_t)prev + tid] += (double)s_f[tid];
 }
 
+// FP32 backward in two kernels.  k_soap_bwd_h: one block per centre forms
+//   h[s][lm][a] = sum_n T_an dE/dc[s][n][lm],  dE/dc[a][lm] = sum_b H_l[a][b] c[b][lm]
+// (H_l the symmetric dE/dp matrices) as k_soap_backward does, into a global buffer.
+// k_soap_bwd_pairs: one thread per pair (all pairs of all centres, so no lane idles
+// at the end of a short neighbour list) walks l and m upwards with everything of the
+// pair in registers (basis sizes fixed at compile time: L = l_max + 1, NMP = n_max
+// padded to 4): the radial functions of all grid points a (upward recurrence
+// rho_{l+1} = rho_{l-1} - (2l+1)/x rho_l) and the Legendre columns of all m (the
+// recurrences of ylm_column_cart, reordered l-outer, their constants in constant
+// memory).  The radial derivative needs no second recurrence: i_l'(x) = i_{l-1}(x) -
+// (l+1)/x i_l(x) gives, for rb > 0,
+//   d rho_l/dr = -(2 alpha r + (l+1)/r) rho_l + 2 alpha rb rho_{l-1},  rho_{-1} = (e- + e+)/2x,
+// so sum_lm w_lm Y_lm = sum_l c_l sum_m u_lm Y_lm + 2 alpha sum_lm v_lm Y_lm with
+// v_lm = sum_a h[lm][a] rb_a rho_{a,l-1} and c_l = -(2 alpha r + (l+1)/r).  The +m and -m
+// entries of one (l, m) share their Legendre factor and the two Cartesian forms, so the
+// sums over lm are taken per (l, m) from U1 = u+ cm + u- sm, V1 = v+ cm + v- sm,
+// Ux = u+ cp + u- sp, Uy = u- cp - u+ sp.  A grid point at rb = 0 contributes
+// exp(-alpha r^2) at l = 0 only and is added to the lm = 0 term.
+constexpr int BH_THREADS = 256;
+constexpr int BP_THREADS = 128;
+constexpr int BH_MAXNN = 24;  // species x n_max of the register-blocked dE/dc rows
+constexpr int MAX_L2 = (MAX_LMAX + 1) * (MAX_LMAX + 1);
+__constant__ float c_lra[MAX_L2], c_lrbb[MAX_L2], c_lyn[MAX_L2];  // by l*l + m, as in the SoapTab
+
+__host__ __device__ __forceinline__ int bh_nnp(const SoapConst& sc) { return (sc.n_species * sc.n_max + 3) & ~3; }
+__host__ __device__ __forceinline__ size_t bh_floats(const SoapConst& sc) {
+    const int L = sc.l_max + 1, c4 = (sc.ncomp + 3) & ~3, p4 = (sc.n_pairs * L + 3) & ~3;
+    return (size_t)soap_tab(sc.n_max, L).size + 2 * (size_t)c4 + (size_t)L * sc.n_species * sc.n_max * bh_nnp(sc) +
+           2 * (size_t)p4;
+}
+
+// Global -> shared copy of n floats by the block with cp.async (no registers held, every
+// copy of the block in flight at once): 16-byte copies where both addresses and n allow,
+// else 4-byte ones.  Completed by cp_async_wait() and a barrier.
+__device__ __forceinline__ void cp_async_floats(float* s, const float* __restrict__ g, int n) {
+    const bool v16 = (((uintptr_t)g | (uintptr_t)s) & 15) == 0 && (n & 3) == 0;
+    if (v16) {
+        for (int k = 4 * (int)threadIdx.x; k < n; k += 4 * (int)blockDim.x)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(s + k)),
+                         "l"(g + k) : "memory");
+    } else {
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(s + k)),
+                         "l"(g + k) : "memory");
+    }
+}
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory"); }
+
+__global__ void __launch_bounds__(BH_THREADS, 4) k_soap_bwd_h(SoapConst sc, const float* __restrict__ tab, int nc,
+                                                           const float* __restrict__ c_in, const float* __restrict__ q_in,
+                                                           const double* __restrict__ pnorm, const float* __restrict__ G,
+                                                           float* __restrict__ hbuf) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ci = blockIdx.x;
+    if (ci >= nc) return;
+    const int L = sc.l_max + 1, L2 = L * L, nm = sc.n_max, NMP = nmp_of(nm), NS = sc.n_species, NN = NS * nm;
+    const int NNP = bh_nnp(sc), ncomp = sc.ncomp, np = sc.n_pairs * L, c4 = (ncomp + 3) & ~3;
+    const SoapTab tb = soap_tab(nm, L);
+    float* K = reinterpret_cast<float*>(smem_raw);
+    float* cs = K + tb.size;  // c[b][lm]
+    float* dc = cs + c4;      // dE/dc[a][lm]
+    float* H = dc + c4;       // H_l[a][b], rows padded to NNP (zero)
+    float* qg = H + L * NN * NNP;             // q and dE/dq of this centre
+    float* gg = qg + ((np + 3) & ~3);
+    __shared__ double s_wsum[BH_THREADS / 32];
+    __shared__ unsigned char lofm[MAX_L2];
+    const int tid = threadIdx.x;
+    cp_async_floats(K, tab, tb.size);
+    cp_async_floats(cs, c_in + (size_t)ci * ncomp, ncomp);
+    cp_async_floats(qg, q_in + (size_t)ci * sc.dpad, np);
+    cp_async_floats(gg, G + (size_t)ci * sc.dpad, np);
+    for (int k = tid; k < L2; k += BH_THREADS) lofm[k] = (unsigned char)l_of_lm(k);
+    if (NNP > NN)
+        for (int k = tid; k < L * NN; k += BH_THREADS)
+            for (int b = NN; b < NNP; ++b) H[k * NNP + b] = 0.f;
+    cp_async_wait();
+    __syncthreads();
+    float part = 0.f;
+    for (int k = tid; k < np; k += BH_THREADS) part += qg[k] * gg[k];
+    part = warp_sum(part);
+    if ((tid & 31) == 0) s_wsum[tid >> 5] = (double)part;
+    __syncthreads();
+    double tot = 0;
+#pragma unroll
+    for (int w = 0; w < BH_THREADS / 32; ++w) tot += s_wsum[w];
+    const float sq = (float)tot, inv = (float)(1.0 / pnorm[ci]);
+    // dE/dp into both triangles of H_l, one power-spectrum row (ia, jb) per thread
+    for (int pr = tid; pr < sc.n_pairs; pr += BH_THREADS) {
+        int ia, jb;
+        decode_pair(pr, ia, jb);
+        const float f0 = ia != jb ? 1.41421356237309504880f : 2.f;
+        for (int l = 0; l < L; ++l) {
+            const int k = pr * L + l;
+            const float g = gg[k];
+            const float v = (sc.normalise ? (g - qg[k] * sq) * inv : g) * f0 * K[tb.lf + l];
+            H[(l * NN + ia) * NNP + jb] = v;
+            H[(l * NN + jb) * NNP + ia] = v;
+        }
+    }
+    __syncthreads();
+    // dE/dc: one item per (lm, 4 rows a), the column c[.][lm] in registers, rows of H_l
+    // as vector loads (broadcast to the threads of one l)
+    const int NA4 = (NN + 3) / 4;
+    for (int it = tid; it < L2 * NA4; it += BH_THREADS) {
+        const int lm = it / NA4, a0 = 4 * (it - lm * NA4), l = lofm[lm];
+        float cb[BH_MAXNN];
+#pragma unroll
+        for (int b = 0; b < BH_MAXNN; ++b) cb[b] = b < NN ? cs[b * L2 + lm] : 0.f;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int a = a0 + r;
+            if (a >= NN) break;
+            const float4* h4 = reinterpret_cast<const float4*>(H + (l * NN + a) * NNP);
+            float x = 0.f;
+#pragma unroll
+            for (int b4 = 0; b4 < BH_MAXNN / 4; ++b4)
+                if (4 * b4 < NNP) {
+                    const float4 hv = h4[b4];
+                    x += hv.x * cb[4 * b4] + hv.y * cb[4 * b4 + 1] + hv.z * cb[4 * b4 + 2] + hv.w * cb[4 * b4 + 3];
+                }
+            dc[a * L2 + lm] = x;
+        }
+    }
+    __syncthreads();
+    // h[s][lm][a] = sum_n T_an dE/dc[s n][lm] (Tp rows past n_max are zero: so is h there)
+    float* ho = hbuf + (size_t)ci * NS * L2 * NMP;
+    for (int it = tid; it < NS * L2; it += BH_THREADS) {
+        const int s = it / L2, lm = it - s * L2;
+        float vn[MAX_NMAX];
+#pragma unroll
+        for (int n = 0; n < MAX_NMAX; ++n) vn[n] = n < nm ? dc[(s * nm + n) * L2 + lm] : 0.f;
+        float4* o = reinterpret_cast<float4*>(ho + (size_t)(s * L2 + lm) * NMP);
+#pragma unroll
+        for (int a4 = 0; a4 < MAX_NMAX / 4; ++a4) {
+            if (4 * a4 >= NMP) break;
+            float x[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const float4* tr = reinterpret_cast<const float4*>(K + tb.Tp + (4 * a4 + r) * NMP);
+                float acc = 0.f;
+#pragma unroll
+                for (int n4 = 0; n4 < MAX_NMAX / 4; ++n4)
+                    if (4 * n4 < NMP) {
+                        const float4 t = tr[n4];
+                        acc += t.x * vn[4 * n4] + t.y * vn[4 * n4 + 1] + t.z * vn[4 * n4 + 2] + t.w * vn[4 * n4 + 3];
+                    }
+                x[r] = acc;
+            }
+            o[a4] = make_float4(x[0], x[1], x[2], x[3]);
+        }
+    }
+}
+
+// a2c[centres[ci]] = ci (the atoms that are no centre keep -1)
+__global__ void k_atom_centre(int nc, const int* __restrict__ centres, int* __restrict__ a2c) {
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci < nc) a2c[centres[ci]] = ci;
+}
+
+template <int L, int NMP>
+__global__ void __launch_bounds__(BP_THREADS, 3) k_soap_bwd_pairs(SoapConst sc, const float* __restrict__ tab, long long npair,
+                                                                const int* __restrict__ a2c, const int* __restrict__ ni,
+                                                                const int* __restrict__ Z, const int* __restrict__ nj,
+                                                                const double4* __restrict__ nd, const float* __restrict__ hbuf,
+                                                                double* __restrict__ fpair) {
+    constexpr int L2 = L * L, NA2 = NMP / 2;
+    const long long p = blockIdx.x * (long long)BP_THREADS + threadIdx.x;
+    if (p >= npair) return;
+    const int ci = a2c[ni[p]];
+    if (ci < 0) return;
+    const double4 d = nd[p];
+    const int s = d.w < sc.rc ? species_channel(sc, Z[nj[p]]) : -1;
+    if (s < 0) return;
+    const int nm = sc.n_max;
+    const SoapTab tb = soap_tab(nm, L);
+    const float alpha = (float)sc.alpha;
+    const float r = (float)d.w, ir = rinv(r);
+    const float ux = (float)d.x * ir, uy = (float)d.y * ir, uz = (float)d.z * ir;
+    float f, df;
+    cutoff_fn<float>(r, (float)sc.rc, (float)sc.w, f, df);
+    const float4* hrow = reinterpret_cast<const float4*>(hbuf + ((size_t)ci * sc.n_species + s) * L2 * NMP);
+    // radial state: rp = rho_{l-1}, rcur = rho_l (pairs of grid points), ix = 1/x, rbv = rb
+    float2 rp[NA2], rcur[NA2];
+    float ix[NMP], rbv[NMP];
+    float e0 = 0.f, h0 = 0.f;  // the rb = 0 grid point, if any (lm = 0 only)
+#pragma unroll
+    for (int a = 0; a < NMP; ++a) {
+        float vm = 0.f, v0 = 0.f, xa = 0.f, rb = 0.f;
+        if (a < nm) {
+            rb = __ldg(tab + tb.rb + a);
+            const float em = rexp(-alpha * (r - rb) * (r - rb));
+            if (rb > 0.f) {
+                const float ep = rexp(-alpha * (r + rb) * (r + rb));
+                xa = rinv(2.f * alpha * r * rb);
+                vm = 0.5f * (em + ep) * xa;
+                v0 = 0.5f * (em - ep) * xa;
+            } else {
+                e0 = em;
+                h0 = __ldg(reinterpret_cast<const float*>(hrow) + a);
+            }
+        }
+        ix[a] = xa;
+        rbv[a] = rb;
+        if (a & 1) { rp[a >> 1].y = vm; rcur[a >> 1].y = v0; }
+        else { rp[a >> 1].x = vm; rcur[a >> 1].x = v0; }
+    }
+    float cm[L], sm[L];
+    cm[0] = 1.f;
+    sm[0] = 0.f;
+#pragma unroll
+    for (int m = 1; m < L; ++m) {
+        cm[m] = cm[m - 1] * ux - sm[m - 1] * uy;
+        sm[m] = sm[m - 1] * ux + cm[m - 1] * uy;
+    }
+    float q1[L], q2[L], d1[L], d2[L];
+#pragma unroll
+    for (int m = 0; m < L; ++m) q1[m] = q2[m] = d1[m] = d2[m] = 0.f;
+    float Auv = 0.f, Awv = 0.f, Avv = 0.f, Ax = 0.f, Ay = 0.f, Az = 0.f;
+    const float t = uz, tar = 2.f * alpha * r;
+    // u = sum_a h[lm][a] rho_a, v = sum_a h[lm][a] rb_a rho_{a,l-1}
+    auto dots = [&](int lm, const float2* pi, float& u, float& v) {
+        float2 uu = make_float2(0.f, 0.f), vv = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < NMP / 4; ++k) {
+            const float4 h = __ldg(hrow + lm * (NMP / 4) + k);
+            const float2 ha = make_float2(h.x, h.y), hb = make_float2(h.z, h.w);
+            uu = __ffma2_rn(ha, rcur[2 * k], uu);
+            vv = __ffma2_rn(ha, pi[2 * k], vv);
+            uu = __ffma2_rn(hb, rcur[2 * k + 1], uu);
+            vv = __ffma2_rn(hb, pi[2 * k + 1], vv);
+        }
+        u = uu.x + uu.y;
+        v = vv.x + vv.y;
+    };
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+        float2 pi[NA2];
+#pragma unroll
+        for (int k = 0; k < NA2; ++k) pi[k] = make_float2(rbv[2 * k] * rp[k].x, rbv[2 * k + 1] * rp[k].y);
+        const int ll = l * l + l;
+        float AuvL = 0.f;
+#pragma unroll
+        for (int m = 0; m <= l; ++m) {
+            float q, dq;
+            if (m == l) {
+                float qmm = 1.f;
+#pragma unroll
+                for (int k = 1; k <= 2 * m - 1; k += 2) qmm *= (float)k;
+                q = qmm;
+                dq = 0.f;
+            } else if (m == l - 1) {
+                q = (float)(2 * m + 1) * t * q1[m];
+                dq = (float)(2 * m + 1) * q1[m];
+            } else {
+                const float ra = c_lra[l * l + m], rbb = c_lrbb[l * l + m];
+                q = ra * t * q1[m] - rbb * q2[m];
+                dq = ra * (q1[m] + t * d1[m]) - rbb * d2[m];
+            }
+            q2[m] = q1[m];
+            q1[m] = q;
+            d2[m] = d1[m];
+            d1[m] = dq;
+            const float nq = c_lyn[l * l + m] * q, ndq = c_lyn[l * l + m] * dq;
+            if (m == 0) {
+                float u, v;
+                dots(ll, pi, u, v);
+                AuvL += nq * u;
+                Avv += nq * v;
+                Az += ndq * u;
+            } else {
+                float up, vp, um, vm;
+                dots(ll + m, pi, up, vp);
+                dots(ll - m, pi, um, vm);
+                const float U1 = up * cm[m] + um * sm[m], V1 = vp * cm[m] + vm * sm[m];
+                const float Ux = up * cm[m - 1] + um * sm[m - 1], Uy = um * cm[m - 1] - up * sm[m - 1];
+                const float am = nq * (float)m;
+                AuvL += nq * U1;
+                Avv += nq * V1;
+                Az += ndq * U1;
+                Ax += am * Ux;
+                Ay += am * Uy;
+            }
+        }
+        Awv += -(tar + (float)(l + 1) * ir) * AuvL;
+        Auv += AuvL;
+        // rho_{l+1} = rho_{l-1} - (2l+1) rho_l / x
+        const float c2 = (float)(2 * l + 1);
+#pragma unroll
+        for (int k = 0; k < NA2; ++k) {
+            const float2 nx = make_float2(rp[k].x - c2 * ix[2 * k] * rcur[k].x, rp[k].y - c2 * ix[2 * k + 1] * rcur[k].y);
+            rp[k] = rcur[k];
+            rcur[k] = nx;
+        }
+    }
+    Awv += 2.f * alpha * Avv;
+    if (h0 != 0.f) {  // rb = 0: rho_0 = exp(-alpha r^2), d rho_0 / dr = -2 alpha r rho_0, Y_00 constant
+        const float y00 = c_lyn[0];
+        Auv += h0 * e0 * y00;
+        Awv += -tar * h0 * e0 * y00;
+    }
+    // f = ar u + (I - u u^T) g / r with ar = sum (f w + f' u) Y, g = f sum u dY/du
+    const float ar = f * Awv + df * Auv, gx = f * Ax, gy = f * Ay, gz = f * Az;
+    const float gu = gx * ux + gy * uy + gz * uz;
+    double* fo = fpair + 3 * p;
+    fo[0] += (double)(ar * ux + (gx - gu * ux) * ir);
+    fo[1] += (double)(ar * uy + (gy - gu * uy) * ir);
+    fo[2] += (double)(ar * uz + (gz - gu * uz) * ir);
+}
+
 __global__ void k_centre_flags(int n, const int* __restrict__ Z, const int* __restrict__ mask, SoapConst sc, int nZ,
                                const int* __restrict__ zlist, int* __restrict__ flags) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -948,8 +1258,55 @@ int launch_forward(gapgpu_context& c, const Coordinate& co, int nc) {
     GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the forward kernel's register accumulators");
 }
 
+template <int L, int NMP>
+int launch_bwd_pairs(gapgpu_context& c, const Coordinate& co, const SoapConst& sc) {
+    const long long P = c.n_pairs;
+    if (P == 0) return GAPGPU_OK;
+    const unsigned nb = (unsigned)((P + BP_THREADS - 1) / BP_THREADS);
+    k_soap_bwd_pairs<L, NMP><<<nb, BP_THREADS, 0, c.stream>>>(sc, static_cast<const float*>(co.dtab[1]), P, c.a2c.as<int>(),
+                                                              c.nbr_i.as<int>(), c.Z.as<int>(), c.nbr_j.as<int>(),
+                                                              c.nbr_d.as<double4>(), c.hbuf.as<float>(),
+                                                              c.fpair.as<double>());
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
+// The two-kernel FP32 backward for the basis sizes the pair kernel is compiled for; -1
+// where it has no instance (the block kernel runs instead).
+int backward_split(gapgpu_context& c, const Coordinate& co, int n, int nc) {
+    const SoapConst sc = soap_const(co);
+    const int NN = sc.n_species * sc.n_max, L = sc.l_max + 1, NMP = nmp_of(sc.n_max);
+    if (NN > BH_MAXNN || sc.n_pairs != NN * (NN + 1) / 2) return -1;
+    int (*pairs)(gapgpu_context&, const Coordinate&, const SoapConst&) = nullptr;
+    if (L == 9 && NMP == 12) pairs = launch_bwd_pairs<9, 12>;
+    else if (L == 7 && NMP == 8) pairs = launch_bwd_pairs<7, 8>;
+    else if (L == 5 && NMP == 8) pairs = launch_bwd_pairs<5, 8>;
+    else if (L == 5 && NMP == 4) pairs = launch_bwd_pairs<5, 4>;
+    if (!pairs) return -1;
+    const size_t sm = sizeof(float) * bh_floats(sc);
+    if (sm > 200 * 1024) return -1;
+    int rc;
+    if ((rc = c.hbuf.ensure(sizeof(float) * (size_t)nc * sc.n_species * L * L * NMP)) ||
+        (rc = c.a2c.ensure(sizeof(int) * (size_t)n)))
+        return rc;
+    GG_CUDA(cudaFuncSetAttribute(k_soap_bwd_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_soap_bwd_h<<<nc, BH_THREADS, sm, c.stream>>>(sc, static_cast<const float*>(co.dtab[1]), nc, c.scratch.as<float>(),
+                                                   c.qbuf.as<float>(), c.pnorm.as<double>(), c.Gbuf.as<float>(),
+                                                   c.hbuf.as<float>());
+    GG_CUDA(cudaMemsetAsync(c.a2c.p, 0xff, sizeof(int) * (size_t)n, c.stream));
+    k_atom_centre<<<(nc + 255) / 256, 256, 0, c.stream>>>(nc, c.cur_centres, c.a2c.as<int>());
+    c.launches += 2;
+    GG_CUDA(cudaGetLastError());
+    return pairs(c, co, sc);
+}
+
 template <class R>
-int launch_backward(gapgpu_context& c, const Coordinate& co, int nc) {
+int launch_backward(gapgpu_context& c, const Coordinate& co, int n, int nc) {
+    if (sizeof(R) == 4 && c.soap_bwd_nb) {
+        const int rc = backward_split(c, co, n, nc);
+        if (rc >= 0) return rc;
+    }
     SoapConst sc = soap_const(co);
     size_t sm = bwd_smem<R>(sc);
     if (sm > 200 * 1024) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the shared-memory backward kernel");
@@ -993,6 +1350,28 @@ int upload_soap_tables(Coordinate& co) {
         }
     }
     std::vector<float> f(h.begin(), h.end());
+    {  // the Legendre constants of the pair kernel for every l <= MAX_LMAX (model independent)
+        static std::once_flag once;
+        static int once_rc = GAPGPU_OK;
+        std::call_once(once, [] {
+            float ra[MAX_L2] = {}, rbb[MAX_L2] = {}, yn[MAX_L2] = {};
+            for (int l = 0; l <= MAX_LMAX; ++l)
+                for (int m = 0; m <= l; ++m) {
+                    double lf = 1.0;
+                    for (int k = l - m + 1; k <= l + m; ++k) lf /= k;
+                    const double N = std::sqrt((2 * l + 1) / (4.0 * M_PI) * lf);
+                    yn[l * l + m] = (float)(m == 0 ? N : std::sqrt(2.0) * N);
+                    if (l >= m + 2) {
+                        ra[l * l + m] = (float)((double)(2 * l - 1) / (double)(l - m));
+                        rbb[l * l + m] = (float)((double)(l + m - 1) / (double)(l - m));
+                    }
+                }
+            if (cudaMemcpyToSymbol(c_lra, ra, sizeof(ra)) != cudaSuccess || cudaMemcpyToSymbol(c_lrbb, rbb, sizeof(rbb)) != cudaSuccess ||
+                cudaMemcpyToSymbol(c_lyn, yn, sizeof(yn)) != cudaSuccess)
+                once_rc = GAPGPU_ERR_CUDA;
+        });
+        if (once_rc != GAPGPU_OK) GG_FAIL(GAPGPU_ERR_CUDA, "uploading the Legendre constants failed");
+    }
     GG_CUDA(cudaMalloc(&co.dtab[0], sizeof(double) * h.size()));
     GG_CUDA(cudaMalloc(&co.dtab[1], sizeof(float) * f.size()));
     GG_CUDA(cudaMemcpy(co.dtab[0], h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
@@ -1047,7 +1426,7 @@ int soap_forward(gapgpu_context& c, const Coordinate& co, int n, int nc) {
 int soap_backward(gapgpu_context& c, const Coordinate& co, int n, int nc) {
     (void)n;
     if (nc == 0) return GAPGPU_OK;
-    return c.precision != GAPGPU_FP64 ? launch_backward<float>(c, co, nc) : launch_backward<double>(c, co, nc);
+    return c.precision != GAPGPU_FP64 ? launch_backward<float>(c, co, n, nc) : launch_backward<double>(c, co, n, nc);
 }
 
 }  // namespace gapgpu

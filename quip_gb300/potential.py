@@ -259,7 +259,9 @@ class Potential:
     def set_option(self, key, value):
         """Context options (gapgpu_context_set_option): graphs (CUDA-graph replay of
         repeated shapes), timing, priority, autotune, pairs (CTA-pair GEMM tiles),
-        gemm1_f16 / gemm2_f16 (the first / second GEMM with FP16 operands on the TF32 path)."""
+        gemm1_f16 / gemm2_f16 (the first / second GEMM with FP16 operands on the TF32 path),
+        soap_bwd (1: the SOAP backward with one thread per pair where the basis has an
+        instance, 0: one block per centre)."""
         _lib.check(self._L.gapgpu_context_set_option(self._ctx, key.encode(), int(value)))
 
     def footprint(self, n_atoms, mean_neighbours=60.0):

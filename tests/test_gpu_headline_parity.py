@@ -12,7 +12,10 @@ oracle at the headline's descriptor size:
 * plain FP64: energy <= 1e-8 eV/atom, forces <= 1e-7 eV/A, virial <= 1e-7 eV;
 * each mixed form (bf16x3, tf32, fp16): forces <= 1 meV/A and energy <= 1e-4 eV/atom;
 * a batch of triclinic Si/C structures (8-256 atoms, log-uniform; lengths 4-30 A,
-  angles 70-110 deg, 1.8 A minimum separation) against per-structure oracle calls.
+  angles 70-110 deg, 1.8 A minimum separation) against per-structure oracle calls;
+* the two FP32 SOAP backward kernels (one thread per pair, the default at this basis
+  size, and one block per centre) on the same structure: the same energy, forces within
+  1e-4 eV/A and virials within 1e-3 eV of each other.
 """
 import os
 
@@ -103,3 +106,16 @@ def test_batch_matches_per_structure_oracle(headline_gap, prec):
         assert np.abs(r["force"] - o["force"]).max() < f_tol
         if prec == "fp64":
             assert np.abs(r["virial"] - o["virial"]).max() < V_TOL
+
+
+@pytest.mark.parametrize("prec", ["fp16", "tf32"])
+def test_backward_kernels_agree(headline_gap, cell, prec):
+    a = _pot(headline_gap, prec)
+    b = _pot(headline_gap, prec)
+    b.set_option("soap_bwd", 0)
+    ra, rb = a.calc(cell), b.calc(cell)
+    df = np.abs(ra["force"] - rb["force"]).max()
+    dv = np.abs(ra["virial"] - rb["virial"]).max()
+    print("%s: thread-per-pair vs block backward: dF=%.2e dV=%.2e" % (prec, df, dv))
+    assert ra["energy"] == rb["energy"]
+    assert df < 1e-4 and dv < 1e-3
