@@ -1048,6 +1048,110 @@ __global__ void __launch_bounds__(BH_THREADS, 4) k_soap_bwd_h(SoapConst sc, cons
     }
 }
 
+// The same h with the basis sizes fixed at compile time (L, NM = n_max, NS species): one
+// thread per lm holds the column c[.][lm] and the accumulators dE/dc[.][lm] in registers
+// and walks the packed dE/dp rows (ia, jb <= ia) unrolled, each entry a broadcast load
+// (dE/dc[ia] += v c[jb], dE/dc[jb] += v c[ia]); T is applied from shared memory and the
+// rows of h go straight to global memory.  No barrier after dE/dp.
+template <int L, int NM, int NS>
+__global__ void __launch_bounds__(((L * L + 31) / 32) * 32) k_soap_bwd_h_lm(SoapConst sc, const float* __restrict__ tab,
+                                                                              int nc, const float* __restrict__ c_in,
+                                                                              const float* __restrict__ q_in,
+                                                                              const double* __restrict__ pnorm,
+                                                                              const float* __restrict__ G,
+                                                                              float* __restrict__ hbuf) {
+    constexpr int L2 = L * L, NN = NS * NM, NMP = (NM + 3) & ~3, NP = NN * (NN + 1) / 2, NPL = NP * L;
+    constexpr int T = ((L2 + 31) / 32) * 32, NW = T / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ci = blockIdx.x;
+    if (ci >= nc) return;
+    const SoapTab tb = soap_tab(NM, L);
+    float* K = reinterpret_cast<float*>(smem_raw);
+    float* qs = K + tb.size;
+    float* gs = qs + ((NPL + 3) & ~3);  // dE/dq, then dE/dp in place
+    __shared__ double s_wsum[NW];
+    const int tid = threadIdx.x, lm = tid;
+    cp_async_floats(K, tab, tb.size);
+    cp_async_floats(qs, q_in + (size_t)ci * sc.dpad, NPL);
+    cp_async_floats(gs, G + (size_t)ci * sc.dpad, NPL);
+    float creg[NN];
+    const float* cg = c_in + (size_t)ci * sc.ncomp;
+#pragma unroll
+    for (int b = 0; b < NN; ++b) creg[b] = lm < L2 ? cg[b * L2 + lm] : 0.f;
+    cp_async_wait();
+    __syncthreads();
+    float part = 0.f;
+    for (int k = tid; k < NPL; k += T) part += qs[k] * gs[k];
+    part = warp_sum(part);
+    if ((tid & 31) == 0) s_wsum[tid >> 5] = (double)part;
+    __syncthreads();
+    double tot = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) tot += s_wsum[w];
+    const float sq = (float)tot, inv = (float)(1.0 / pnorm[ci]);
+    for (int pr = tid; pr < NP; pr += T) {
+        int ia, jb;
+        decode_pair(pr, ia, jb);
+        const float f0 = ia != jb ? 1.41421356237309504880f : 2.f;
+#pragma unroll
+        for (int l = 0; l < L; ++l) {
+            const int k = pr * L + l;
+            const float g = gs[k];
+            gs[k] = (sc.normalise ? (g - qs[k] * sq) * inv : g) * f0 * K[tb.lf + l];
+        }
+    }
+    __syncthreads();
+    if (lm >= L2) return;
+    const int l = l_of_lm(lm);
+    float dreg[NN];
+#pragma unroll
+    for (int a = 0; a < NN; ++a) dreg[a] = 0.f;
+    const float* dp = gs + l;
+#pragma unroll
+    for (int ia = 0; ia < NN; ++ia)
+#pragma unroll
+        for (int jb = 0; jb <= ia; ++jb) {
+            const float v = dp[(ia * (ia + 1) / 2 + jb) * L];
+            dreg[ia] += v * creg[jb];
+            if (ia != jb) dreg[jb] += v * creg[ia];
+        }
+    float* ho = hbuf + (size_t)ci * NS * L2 * NMP;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        float x[NMP];
+#pragma unroll
+        for (int a = 0; a < NMP; ++a) {
+            const float4* tr = reinterpret_cast<const float4*>(K + tb.Tp + a * NMP);
+            float acc = 0.f;
+#pragma unroll
+            for (int n4 = 0; n4 < NMP / 4; ++n4) {
+                const float4 t = tr[n4];
+                const float tv[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (4 * n4 + e < NM) acc += tv[e] * dreg[s * NM + 4 * n4 + e];
+            }
+            x[a] = acc;
+        }
+        float4* o = reinterpret_cast<float4*>(ho + (size_t)(s * L2 + lm) * NMP);
+#pragma unroll
+        for (int a4 = 0; a4 < NMP / 4; ++a4) o[a4] = make_float4(x[4 * a4], x[4 * a4 + 1], x[4 * a4 + 2], x[4 * a4 + 3]);
+    }
+}
+
+template <int L, int NM, int NS>
+int launch_bwd_h_lm(gapgpu_context& c, const Coordinate& co, int nc, const SoapConst& sc) {
+    constexpr int NN = NS * NM, NPL = NN * (NN + 1) / 2 * L, T = ((L * L + 31) / 32) * 32;
+    const size_t sm = sizeof(float) * ((size_t)soap_tab(NM, L).size + 2 * (size_t)((NPL + 3) & ~3));
+    GG_CUDA(cudaFuncSetAttribute(k_soap_bwd_h_lm<L, NM, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_soap_bwd_h_lm<L, NM, NS><<<nc, T, sm, c.stream>>>(sc, static_cast<const float*>(co.dtab[1]), nc, c.scratch.as<float>(),
+                                                        c.qbuf.as<float>(), c.pnorm.as<double>(), c.Gbuf.as<float>(),
+                                                        c.hbuf.as<float>());
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
 // a2c[centres[ci]] = ci (the atoms that are no centre keep -1)
 __global__ void k_atom_centre(int nc, const int* __restrict__ centres, int* __restrict__ a2c) {
     const int ci = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1290,13 +1394,21 @@ int backward_split(gapgpu_context& c, const Coordinate& co, int n, int nc) {
     if ((rc = c.hbuf.ensure(sizeof(float) * (size_t)nc * sc.n_species * L * L * NMP)) ||
         (rc = c.a2c.ensure(sizeof(int) * (size_t)n)))
         return rc;
-    GG_CUDA(cudaFuncSetAttribute(k_soap_bwd_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_soap_bwd_h<<<nc, BH_THREADS, sm, c.stream>>>(sc, static_cast<const float*>(co.dtab[1]), nc, c.scratch.as<float>(),
-                                                   c.qbuf.as<float>(), c.pnorm.as<double>(), c.Gbuf.as<float>(),
-                                                   c.hbuf.as<float>());
+    const int nm = sc.n_max, ns = sc.n_species;
+    if (L == 9 && nm == 10 && ns == 2) rc = launch_bwd_h_lm<9, 10, 2>(c, co, nc, sc);
+    else if (L == 7 && nm == 8 && ns == 1) rc = launch_bwd_h_lm<7, 8, 1>(c, co, nc, sc);
+    else if (L == 5 && nm == 4 && ns == 2) rc = launch_bwd_h_lm<5, 4, 2>(c, co, nc, sc);
+    else {
+        GG_CUDA(cudaFuncSetAttribute(k_soap_bwd_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_soap_bwd_h<<<nc, BH_THREADS, sm, c.stream>>>(sc, static_cast<const float*>(co.dtab[1]), nc, c.scratch.as<float>(),
+                                                       c.qbuf.as<float>(), c.pnorm.as<double>(), c.Gbuf.as<float>(),
+                                                       c.hbuf.as<float>());
+        c.launches++;
+    }
+    if (rc) return rc;
     GG_CUDA(cudaMemsetAsync(c.a2c.p, 0xff, sizeof(int) * (size_t)n, c.stream));
     k_atom_centre<<<(nc + 255) / 256, 256, 0, c.stream>>>(nc, c.cur_centres, c.a2c.as<int>());
-    c.launches += 2;
+    c.launches++;
     GG_CUDA(cudaGetLastError());
     return pairs(c, co, sc);
 }
