@@ -1161,14 +1161,19 @@ __global__ void k_atom_centre(int nc, const int* __restrict__ centres, int* __re
 template <int L, int NMP>
 __global__ void __launch_bounds__(BP_THREADS, 3) k_soap_bwd_pairs(SoapConst sc, const float* __restrict__ tab, long long npair,
                                                                 const int* __restrict__ a2c, const int* __restrict__ ni,
-                                                                const int* __restrict__ Z, const int* __restrict__ nj,
-                                                                const double4* __restrict__ nd, const float* __restrict__ hbuf,
-                                                                double* __restrict__ fpair) {
+                                                                const int* __restrict__ off, const int* __restrict__ Z,
+                                                                const int* __restrict__ nj, const double4* __restrict__ nd,
+                                                                const float* __restrict__ hbuf, double* __restrict__ fpair) {
     constexpr int L2 = L * L, NA2 = NMP / 2;
     const long long p = blockIdx.x * (long long)BP_THREADS + threadIdx.x;
     if (p >= npair) return;
-    const int ci = a2c[ni[p]];
+    const int ai = ni[p], ci = a2c[ai];
     if (ci < 0) return;
+    {  // the centre's h block into L1, its 128-byte lines shared out over the centre's pairs
+        const int p0 = off[ai], cnt = off[ai + 1] - p0, lines = (sc.n_species * L2 * NMP * 4 + 127) / 128;
+        const char* hb = reinterpret_cast<const char*>(hbuf + (size_t)ci * sc.n_species * L2 * NMP);
+        for (int k = (int)(p - p0); k < lines; k += cnt) asm volatile("prefetch.L1 [%0];" ::"l"(hb + 128 * (size_t)k));
+    }
     const double4 d = nd[p];
     const int s = d.w < sc.rc ? species_channel(sc, Z[nj[p]]) : -1;
     if (s < 0) return;
@@ -1368,7 +1373,8 @@ int launch_bwd_pairs(gapgpu_context& c, const Coordinate& co, const SoapConst& s
     if (P == 0) return GAPGPU_OK;
     const unsigned nb = (unsigned)((P + BP_THREADS - 1) / BP_THREADS);
     k_soap_bwd_pairs<L, NMP><<<nb, BP_THREADS, 0, c.stream>>>(sc, static_cast<const float*>(co.dtab[1]), P, c.a2c.as<int>(),
-                                                              c.nbr_i.as<int>(), c.Z.as<int>(), c.nbr_j.as<int>(),
+                                                              c.nbr_i.as<int>(), c.nbr_off.as<int>(), c.Z.as<int>(),
+                                                              c.nbr_j.as<int>(),
                                                               c.nbr_d.as<double4>(), c.hbuf.as<float>(),
                                                               c.fpair.as<double>());
     c.launches++;
