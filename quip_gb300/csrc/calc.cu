@@ -612,6 +612,7 @@ int gapgpu_context_set_option(gapgpu_context* c, const char* key, int value) {
     else if (k == "gemm2_f16") c->gemm2_f16 = value != 0;
     else if (k == "gemm1_f16") c->gemm1_f16 = value != 0;
     else if (k == "soap_bwd") c->soap_bwd_nb = value != 0;
+    else if (k == "soap_fwd") c->soap_fwd_fixed = value != 0;
     else if (k == "pairs") {
         if (value < 0 || value > 2) GG_FAIL(GAPGPU_ERR_ARG, "gapgpu_context_set_option: pairs must be 0, 1 or 2");
         c->gemm_pairs = value;

@@ -91,6 +91,7 @@ struct gapgpu_context {
     int graph_mode = 0;                       // 0: never, 1: capture on the second identical call
     bool autotune = true;                     // time the GEMM tile candidates of a new shape once
     int gemm_pairs = 1;                       // CTA-pair GEMM tiles: 0 off, 1 autotuner candidates, 2 only
+    int soap_fwd_fixed = 1;                   // FP32 SOAP forward: 1 the fixed-size kernel where the basis has an instance
     int soap_bwd_nb = 1;                      // FP32 SOAP backward: 1 h kernel + one thread per pair where the basis allows, 0 one block per centre
     bool gemm2_f16 = false;                   // TF32 mode: FP16 second GEMM where the model allows it
     bool gemm1_f16 = false;                   // ... and FP16 first GEMM (on for GAPGPU_MIXED_F16 contexts)

@@ -1313,6 +1313,341 @@ __global__ void __launch_bounds__(BP_THREADS, 3) k_soap_bwd_pairs(SoapConst sc, 
     fo[2] += (double)(ar * uz + (gz - gu * uz) * ir);
 }
 
+// Forward with the basis sizes fixed at compile time (L = l_max + 1, NMP = n_max padded to
+// 4; FP32): the accumulation and the per-centre tail of k_soap_forward, with
+//  * the neighbour functions of a chunk computed one thread per staged neighbour with the
+//    whole state in registers: warp 0 the radial rows of all grid points (upward Bessel
+//    recurrence, l outermost, four grid points per store), warp 1 the Ylm of all (l, m)
+//    (the Legendre columns of all m advanced together, constants in constant memory);
+//  * one accumulator item per thread: (species, up to three m of one l, four grid points),
+//    so each staged radial quadruple feeds up to 12 products;
+//  * q, its GEMM-operand copy and c written as vectors.
+__host__ __device__ constexpr int fwd_triples(int L) {
+    int t = 0;
+    for (int l = 0; l < L; ++l) t += (2 * l + 1 + 2) / 3;
+    return t;
+}
+
+template <int L, int NMP>
+__global__ void __launch_bounds__(FWD_THREADS, 4) k_soap_fwd_t(SoapConst sc, const float* __restrict__ tab, int nc,
+                                                             const int* __restrict__ centres, const int* __restrict__ Z,
+                                                             const int* __restrict__ off, const int* __restrict__ nj,
+                                                             const double4* __restrict__ nd, float* __restrict__ c_out,
+                                                             float* __restrict__ q_out, void* __restrict__ qr_out,
+                                                             int qr_half, double* __restrict__ pnorm) {
+    constexpr int L2 = L * L, NA4 = NMP / 4, NA2 = NMP / 2, NT = fwd_triples(L);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ci = blockIdx.x;
+    if (ci >= nc) return;
+    const int atom = centres[ci];
+    const int nm = sc.n_max, NS = sc.n_species;
+    const SoapTab tb = soap_tab(nm, L);
+    float* K = reinterpret_cast<float*>(smem_raw);
+    float* cs = K + tb.size;                          // NS * nm * L2
+    float* Ysm = cs + ((NS * nm * L2 + 3) & ~3);      // TC * L2
+    float* Ism = Ysm + TC * L2;                       // TC * L * NMP
+    float* fcs = Ism + TC * L * NMP;                  // TC
+    float* dsm = fcs + TC;                            // TC * DS
+    float* ct = Ysm;                                  // NS * L2 * NMP, after the loop
+    const int region = fwd_region(sc);
+    int* spc = reinterpret_cast<int*>(Ysm + region);  // TC
+    int* lst = spc + TC;                              // NS * TC
+    int* lcnt = lst + NS * TC;                        // NS
+    const int tid = threadIdx.x, bd = blockDim.x;
+    copy_to_smem<4>(tab, K, tb.size);
+    // this thread's item: species s, lm0 .. lm0 + cnt - 1 (one l), grid points 4 a4 .. 4 a4 + 3
+    int own_s = -1, own_l = 0, own_lm0 = 0, own_cnt = 0, own_a4 = 0;
+    if (tid < NS * NT * NA4) {
+        own_s = tid / (NT * NA4);
+        const int rem = tid - own_s * NT * NA4, tr = rem / NA4;
+        own_a4 = rem - tr * NA4;
+        int k = tr;
+        for (int l = 0; l < L; ++l) {
+            const int n3 = (2 * l + 1 + 2) / 3;
+            if (k < n3) {
+                own_l = l;
+                own_lm0 = l * l + 3 * k;
+                own_cnt = min(3, 2 * l + 1 - 3 * k);
+                break;
+            }
+            k -= n3;
+        }
+    }
+    float acc[3][4];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.f;
+    const float alpha = (float)sc.alpha;
+    const int p0 = off[atom], p1 = off[atom + 1];
+    for (int base = p0; base < p1; base += TC) {
+        const int cnt = min(TC, p1 - base);
+        __syncthreads();
+        {
+            ChunkFetch nf;
+            nf.load<TC>(base, p1, Z, nj, nd);
+            if (tid < 32) build_species_lists<TC>(sc, cnt, nf, spc, lst, lcnt);
+            else if (tid - 32 < cnt) {
+                const int t = tid - 32;
+                stage_neighbour<float>(sc, nf.d, dsm + DS * t, fcs + t, (float*)nullptr);
+            }
+        }
+        __syncthreads();
+        {
+            const int t = tid & 31, wid = tid >> 5;
+            if (wid < 2 && t < cnt && spc[t] >= 0) {
+                const float* u = dsm + DS * t;
+                const float r = u[4], fc = fcs[t];
+                if (wid == 0) {  // radial rows: fc rho_{a,l}(r) for all a, l
+                    float2 rp[NA2], rcur[NA2];
+                    float ix[NMP];
+#pragma unroll
+                    for (int a = 0; a < NMP; ++a) {
+                        float vm = 0.f, v0 = 0.f, xa = 0.f;
+                        if (a < nm) {
+                            const float rb = K[tb.rb + a];
+                            const float em = rexp(-alpha * (r - rb) * (r - rb));
+                            if (rb > 0.f) {
+                                const float ep = rexp(-alpha * (r + rb) * (r + rb));
+                                xa = rinv(2.f * alpha * r * rb);
+                                vm = 0.5f * (em + ep) * xa;
+                                v0 = 0.5f * (em - ep) * xa;
+                            } else {
+                                v0 = em;  // rb = 0: rho_0 = exp(-alpha r^2), rho_l = 0 for l > 0
+                            }
+                        }
+                        ix[a] = xa;
+                        if (a & 1) { rp[a >> 1].y = vm; rcur[a >> 1].y = v0; }
+                        else { rp[a >> 1].x = vm; rcur[a >> 1].x = v0; }
+                    }
+                    float4* row = reinterpret_cast<float4*>(Ism + t * L * NMP);
+#pragma unroll
+                    for (int l = 0; l < L; ++l) {
+#pragma unroll
+                        for (int k4 = 0; k4 < NA4; ++k4)
+                            row[l * NA4 + k4] = make_float4(fc * rcur[2 * k4].x, fc * rcur[2 * k4].y, fc * rcur[2 * k4 + 1].x,
+                                                            fc * rcur[2 * k4 + 1].y);
+                        const float c2 = (float)(2 * l + 1);
+#pragma unroll
+                        for (int k = 0; k < NA2; ++k) {
+                            const float2 nx = make_float2(rp[k].x - c2 * ix[2 * k] * rcur[k].x,
+                                                          rp[k].y - c2 * ix[2 * k + 1] * rcur[k].y);
+                            rp[k] = rcur[k];
+                            rcur[k] = nx;
+                        }
+                        if (l == 0) {  // the rb = 0 point stops after l = 0
+#pragma unroll
+                            for (int a = 0; a < NMP; ++a)
+                                if (a < nm && K[tb.rb + a] == 0.f) {
+                                    if (a & 1) rp[a >> 1].y = 0.f;
+                                    else rp[a >> 1].x = 0.f;
+                                }
+                        }
+                    }
+                } else {  // Ylm of all (l, m)
+                    const float ux = u[0], uy = u[1], t3 = u[2];
+                    float cm[L], sm[L], q1[L], q2[L];
+                    cm[0] = 1.f;
+                    sm[0] = 0.f;
+#pragma unroll
+                    for (int m = 1; m < L; ++m) {
+                        cm[m] = cm[m - 1] * ux - sm[m - 1] * uy;
+                        sm[m] = sm[m - 1] * ux + cm[m - 1] * uy;
+                    }
+#pragma unroll
+                    for (int m = 0; m < L; ++m) q1[m] = q2[m] = 0.f;
+                    float* Y = Ysm + t * L2;
+#pragma unroll
+                    for (int l = 0; l < L; ++l)
+#pragma unroll
+                        for (int m = 0; m <= l; ++m) {
+                            float q;
+                            if (m == l) {
+                                float qmm = 1.f;
+#pragma unroll
+                                for (int k = 1; k <= 2 * m - 1; k += 2) qmm *= (float)k;
+                                q = qmm;
+                            } else if (m == l - 1) {
+                                q = (float)(2 * m + 1) * t3 * q1[m];
+                            } else {
+                                q = c_lra[l * l + m] * t3 * q1[m] - c_lrbb[l * l + m] * q2[m];
+                            }
+                            q2[m] = q1[m];
+                            q1[m] = q;
+                            const float nq = c_lyn[l * l + m] * q;
+                            if (m == 0) Y[l * l + l] = nq;
+                            else {
+                                Y[l * l + l + m] = nq * cm[m];
+                                Y[l * l + l - m] = nq * sm[m];
+                            }
+                        }
+                }
+            }
+        }
+        __syncthreads();
+        if (own_s >= 0) {
+            const int nt = lcnt[own_s];
+            const int* ls = lst + own_s * TC;
+            for (int qq = 0; qq < nt; ++qq) {
+                const int t = ls[qq];
+                const float4 rho = *reinterpret_cast<const float4*>(Ism + (t * L + own_l) * NMP + 4 * own_a4);
+                const float* yv = Ysm + t * L2 + own_lm0;
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    if (k < own_cnt) {
+                        const float y = yv[k];
+                        acc[k][0] += y * rho.x;
+                        acc[k][1] += y * rho.y;
+                        acc[k][2] += y * rho.z;
+                        acc[k][3] += y * rho.w;
+                    }
+            }
+        }
+    }
+    __syncthreads();  // the staging area becomes ct
+    if (own_s >= 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (k < own_cnt)
+                *reinterpret_cast<float4*>(ct + (own_s * L2 + own_lm0 + k) * NMP + 4 * own_a4) =
+                    make_float4(acc[k][0], acc[k][1], acc[k][2], acc[k][3]);
+    }
+    __syncthreads();
+    // c[s][n][lm] = sum_a T_an ct[s][lm][a]  (+ central atom at l = 0): one thread per (s, lm)
+    const int zc = Z[atom];
+    for (int k = tid; k < NS * L2; k += bd) {
+        const int s = k / L2, lm = k - s * L2;
+        const float4* v4 = reinterpret_cast<const float4*>(ct + (s * L2 + lm) * NMP);
+        float va[NMP];
+#pragma unroll
+        for (int a4 = 0; a4 < NA4; ++a4) {
+            const float4 w = v4[a4];
+            va[4 * a4] = w.x; va[4 * a4 + 1] = w.y; va[4 * a4 + 2] = w.z; va[4 * a4 + 3] = w.w;
+        }
+        const bool centre = lm == 0 && (sc.centre_all || sc.species_Z[s] == zc || sc.species_Z[s] == 0);
+        for (int n = 0; n < nm; ++n) {
+            const float4* tr = reinterpret_cast<const float4*>(K + tb.Tt + n * NMP);
+            float x = 0.f;
+#pragma unroll
+            for (int a4 = 0; a4 < NA4; ++a4) {
+                const float4 w = tr[a4];
+                x += w.x * va[4 * a4] + w.y * va[4 * a4 + 1] + w.z * va[4 * a4 + 2] + w.w * va[4 * a4 + 3];
+            }
+            if (centre) x += K[tb.cr + n];
+            cs[(s * nm + n) * L2 + lm] = x;
+        }
+    }
+    __syncthreads();
+    {
+        float* cg = c_out + (size_t)ci * sc.ncomp;
+        if ((sc.ncomp & 3) == 0) {
+            for (int k = tid; k < sc.ncomp / 4; k += bd)
+                reinterpret_cast<float4*>(cg)[k] = reinterpret_cast<const float4*>(cs)[k];
+        } else {
+            for (int k = tid; k < sc.ncomp; k += bd) cg[k] = cs[k];
+        }
+    }
+    // power spectrum: one item per (l, 2x2 block of channel rows (ia, jb), ia >= jb)
+    float* ps = Ysm;
+    float ssr = 0.f;
+    {
+        const int NR = NS * nm, NB = (NR + 1) / 2, nblk = NB * (NB + 1) / 2;
+        if (tid < nblk * L) {
+            Walk2 w(tid, bd, nblk);
+            for (; w.i < L; w.next()) {
+                const int l = w.i;
+                int bi = (int)((sqrtf((float)(8 * w.j + 1)) - 1.0f) * 0.5f);
+                while ((bi + 1) * (bi + 2) / 2 <= w.j) ++bi;
+                while (bi * (bi + 1) / 2 > w.j) --bi;
+                const int bj = w.j - bi * (bi + 1) / 2;
+                const int i0 = 2 * bi, j0 = 2 * bj;
+                const bool i1ok = i0 + 1 < NR, j1ok = j0 + 1 < NR;
+                const float* a0 = cs + i0 * L2 + l * l;
+                const float* a1 = cs + (i1ok ? i0 + 1 : i0) * L2 + l * l;
+                const float* b0 = cs + j0 * L2 + l * l;
+                const float* b1 = cs + (j1ok ? j0 + 1 : j0) * L2 + l * l;
+                float v00 = 0.f, v01 = 0.f, v10 = 0.f, v11 = 0.f;
+                for (int m = 0; m < 2 * l + 1; ++m) {
+                    const float x0 = a0[m], x1 = a1[m], y0 = b0[m], y1 = b1[m];
+                    v00 += x0 * y0;
+                    v01 += x0 * y1;
+                    v10 += x1 * y0;
+                    v11 += x1 * y1;
+                }
+                const float lf = K[tb.lf + l], r2 = 1.41421356237309504880f;
+                auto put = [&](int ia, int jb, float v) {
+                    v *= (ia != jb ? r2 : 1.f) * lf;
+                    ps[(ia * (ia + 1) / 2 + jb) * L + l] = v;
+                    ssr += v * v;
+                };
+                put(i0, j0, v00);
+                if (j1ok && bi != bj) put(i0, j0 + 1, v01);
+                if (i1ok) put(i0 + 1, j0, v10);
+                if (i1ok && j1ok) put(i0 + 1, j0 + 1, v11);
+            }
+        }
+    }
+    __shared__ double s_wsum[FWD_THREADS / 32];
+    __shared__ float s_inv;
+    ssr = warp_sum(ssr);
+    if ((tid & 31) == 0) s_wsum[tid >> 5] = (double)ssr;
+    __syncthreads();
+    if (tid == 0) {
+        double tot = 0;
+        for (int w = 0; w < FWD_THREADS / 32; ++w) tot += s_wsum[w];
+        const double nrm = sqrt(tot);
+        pnorm[ci] = nrm;
+        s_inv = sc.normalise ? (float)(1.0 / nrm) : 1.f;
+    }
+    __syncthreads();
+    const float inv = s_inv, sig = (float)sc.sigma0;
+    const int np = sc.n_pairs * L;
+    float* qg = q_out + (size_t)ci * sc.dpad;
+    float* qrg = qr_out && !qr_half ? static_cast<float*>(qr_out) + (size_t)ci * sc.dpad : nullptr;
+    __half* qhg = qr_out && qr_half ? static_cast<__half*>(qr_out) + (size_t)ci * sc.dpad : nullptr;
+    for (int k4 = tid; k4 < sc.dpad / 4; k4 += bd) {  // dpad is a multiple of 4
+        float v[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int k = 4 * k4 + e;
+            v[e] = k < np ? ps[k] * inv : (k == np ? sig : 0.f);
+        }
+        reinterpret_cast<float4*>(qg)[k4] = make_float4(v[0], v[1], v[2], v[3]);
+        if (qrg)
+            __stcs(reinterpret_cast<float4*>(qrg) + k4,
+                   make_float4(round_tf32(v[0]), round_tf32(v[1]), round_tf32(v[2]), round_tf32(v[3])));
+        if (qhg) {
+            const __half2 h0 = __floats2half2_rn(v[0], v[1]), h1 = __floats2half2_rn(v[2], v[3]);
+            uint2 pk;
+            pk.x = *reinterpret_cast<const unsigned*>(&h0);
+            pk.y = *reinterpret_cast<const unsigned*>(&h1);
+            reinterpret_cast<uint2*>(qhg)[k4] = pk;
+        }
+    }
+}
+
+template <int L, int NMP>
+int launch_fwd_t(gapgpu_context& c, const Coordinate& co, int nc, const SoapConst& sc, size_t sm) {
+    GG_CUDA(cudaFuncSetAttribute(k_soap_fwd_t<L, NMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_soap_fwd_t<L, NMP><<<nc, FWD_THREADS, sm, c.stream>>>(
+        sc, static_cast<const float*>(co.dtab[1]), nc, c.cur_centres, c.Z.as<int>(), c.nbr_off.as<int>(), c.nbr_j.as<int>(),
+        c.nbr_d.as<double4>(), c.scratch.as<float>(), c.qbuf.as<float>(),
+        c.precision == GAPGPU_MIXED_TF32 ? c.qlo.p : nullptr, gemm1_f16_active(c, co) ? 1 : 0, c.pnorm.as<double>());
+    c.launches++;
+    GG_CUDA(cudaGetLastError());
+    return GAPGPU_OK;
+}
+
+// The fixed-size FP32 forward where it has an instance (-1 otherwise).
+int forward_fixed(gapgpu_context& c, const Coordinate& co, int nc, const SoapConst& sc, size_t sm) {
+    const int L = sc.l_max + 1, NMP = nmp_of(sc.n_max);
+    if ((sc.dpad & 3) != 0) return -1;
+    auto fits = [&](int T, int na4) { return sc.n_species * T * na4 <= FWD_THREADS; };
+    if (L == 9 && NMP == 12 && fits(fwd_triples(9), 3)) return launch_fwd_t<9, 12>(c, co, nc, sc, sm);
+    if (L == 7 && NMP == 8 && fits(fwd_triples(7), 2)) return launch_fwd_t<7, 8>(c, co, nc, sc, sm);
+    if (L == 5 && NMP == 8 && fits(fwd_triples(5), 2)) return launch_fwd_t<5, 8>(c, co, nc, sc, sm);
+    if (L == 5 && NMP == 4 && fits(fwd_triples(5), 1)) return launch_fwd_t<5, 4>(c, co, nc, sc, sm);
+    return -1;
+}
+
 __global__ void k_centre_flags(int n, const int* __restrict__ Z, const int* __restrict__ mask, SoapConst sc, int nZ,
                                const int* __restrict__ zlist, int* __restrict__ flags) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1361,6 +1696,10 @@ int launch_forward(gapgpu_context& c, const Coordinate& co, int nc) {
     SoapConst sc = soap_const(co);
     size_t sm = fwd_smem<R>(sc);
     if (sm > 200 * 1024) GG_FAIL(GAPGPU_ERR_UNSUPPORTED, "SOAP basis too large for the shared-memory forward kernel");
+    if (sizeof(R) == 4 && c.soap_fwd_fixed) {
+        const int rc = forward_fixed(c, co, nc, sc, sm);
+        if (rc >= 0) return rc;
+    }
     const int items = sc.n_species * (sc.l_max + 1) * (sc.l_max + 1) * (nmp_of(sc.n_max) / 4);
     if (items <= FQ_SMALL * FWD_THREADS) return launch_forward_fq<R, FQ_SMALL>(c, co, nc, sc, sm);
     if (items <= FQ_LARGE * FWD_THREADS) return launch_forward_fq<R, FQ_LARGE>(c, co, nc, sc, sm);

@@ -261,7 +261,8 @@ class Potential:
         repeated shapes), timing, priority, autotune, pairs (CTA-pair GEMM tiles),
         gemm1_f16 / gemm2_f16 (the first / second GEMM with FP16 operands on the TF32 path),
         soap_bwd (1: the SOAP backward with one thread per pair where the basis has an
-        instance, 0: one block per centre)."""
+        instance, 0: one block per centre), soap_fwd (1: the fixed-size SOAP forward where
+        the basis has an instance, 0: the generic one)."""
         _lib.check(self._L.gapgpu_context_set_option(self._ctx, key.encode(), int(value)))
 
     def footprint(self, n_atoms, mean_neighbours=60.0):

@@ -15,7 +15,9 @@ oracle at the headline's descriptor size:
   angles 70-110 deg, 1.8 A minimum separation) against per-structure oracle calls;
 * the two FP32 SOAP backward kernels (one thread per pair, the default at this basis
   size, and one block per centre) on the same structure: the same energy, forces within
-  1e-4 eV/A and virials within 1e-3 eV of each other.
+  1e-4 eV/A and virials within 1e-3 eV of each other;
+* the two FP32 SOAP forward kernels (fixed basis size, the default here, and the generic
+  one): energies within 1e-6 eV/atom, forces within 1e-4 eV/A of each other.
 """
 import os
 
@@ -119,3 +121,15 @@ def test_backward_kernels_agree(headline_gap, cell, prec):
     print("%s: thread-per-pair vs block backward: dF=%.2e dV=%.2e" % (prec, df, dv))
     assert ra["energy"] == rb["energy"]
     assert df < 1e-4 and dv < 1e-3
+
+
+@pytest.mark.parametrize("prec", ["fp16", "tf32"])
+def test_forward_kernels_agree(headline_gap, cell, prec):
+    a = _pot(headline_gap, prec)
+    b = _pot(headline_gap, prec)
+    b.set_option("soap_fwd", 0)
+    ra, rb = a.calc(cell), b.calc(cell)
+    de = abs(ra["energy"] - rb["energy"]) / len(cell)
+    df = np.abs(ra["force"] - rb["force"]).max()
+    print("%s: fixed-size vs generic forward: dE/atom=%.2e dF=%.2e" % (prec, de, df))
+    assert de < 1e-6 and df < 1e-4
