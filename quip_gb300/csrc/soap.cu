@@ -1392,16 +1392,21 @@ __global__ void __launch_bounds__(FWD_THREADS, 4) k_soap_fwd_t(SoapConst sc, con
         }
         __syncthreads();
         {
+            // warps 0 .. NA4-1: the radial rows of one quadruple of grid points each; the other
+            // warps: Ylm columns m with m mod 2W in {j, 2W-1-j} (W column warps, j = warp - NA4),
+            // which gives every column warp the same number of Legendre steps
             const int t = tid & 31, wid = tid >> 5;
-            if (wid < 2 && t < cnt && spc[t] >= 0) {
+            if (t < cnt && spc[t] >= 0) {
                 const float* u = dsm + DS * t;
                 const float r = u[4], fc = fcs[t];
-                if (wid == 0) {  // radial rows: fc rho_{a,l}(r) for all a, l
-                    float2 rp[NA2], rcur[NA2];
-                    float ix[NMP];
+                if (wid < NA4) {
+                    float rp[4], rcur[4], ix[4];
+                    bool rb0[4];
 #pragma unroll
-                    for (int a = 0; a < NMP; ++a) {
+                    for (int e = 0; e < 4; ++e) {
+                        const int a = 4 * wid + e;
                         float vm = 0.f, v0 = 0.f, xa = 0.f;
+                        rb0[e] = false;
                         if (a < nm) {
                             const float rb = K[tb.rb + a];
                             const float em = rexp(-alpha * (r - rb) * (r - rb));
@@ -1412,73 +1417,31 @@ __global__ void __launch_bounds__(FWD_THREADS, 4) k_soap_fwd_t(SoapConst sc, con
                                 v0 = 0.5f * (em - ep) * xa;
                             } else {
                                 v0 = em;  // rb = 0: rho_0 = exp(-alpha r^2), rho_l = 0 for l > 0
+                                rb0[e] = true;
                             }
                         }
-                        ix[a] = xa;
-                        if (a & 1) { rp[a >> 1].y = vm; rcur[a >> 1].y = v0; }
-                        else { rp[a >> 1].x = vm; rcur[a >> 1].x = v0; }
+                        rp[e] = vm;
+                        rcur[e] = v0;
+                        ix[e] = xa;
                     }
-                    float4* row = reinterpret_cast<float4*>(Ism + t * L * NMP);
+                    float4* row = reinterpret_cast<float4*>(Ism + t * L * NMP) + wid;
 #pragma unroll
                     for (int l = 0; l < L; ++l) {
-#pragma unroll
-                        for (int k4 = 0; k4 < NA4; ++k4)
-                            row[l * NA4 + k4] = make_float4(fc * rcur[2 * k4].x, fc * rcur[2 * k4].y, fc * rcur[2 * k4 + 1].x,
-                                                            fc * rcur[2 * k4 + 1].y);
+                        row[l * NA4] = make_float4(fc * rcur[0], fc * rcur[1], fc * rcur[2], fc * rcur[3]);
                         const float c2 = (float)(2 * l + 1);
 #pragma unroll
-                        for (int k = 0; k < NA2; ++k) {
-                            const float2 nx = make_float2(rp[k].x - c2 * ix[2 * k] * rcur[k].x,
-                                                          rp[k].y - c2 * ix[2 * k + 1] * rcur[k].y);
-                            rp[k] = rcur[k];
-                            rcur[k] = nx;
-                        }
-                        if (l == 0) {  // the rb = 0 point stops after l = 0
-#pragma unroll
-                            for (int a = 0; a < NMP; ++a)
-                                if (a < nm && K[tb.rb + a] == 0.f) {
-                                    if (a & 1) rp[a >> 1].y = 0.f;
-                                    else rp[a >> 1].x = 0.f;
-                                }
+                        for (int e = 0; e < 4; ++e) {
+                            const float nx = rp[e] - c2 * ix[e] * rcur[e];
+                            rp[e] = (l == 0 && rb0[e]) ? 0.f : rcur[e];
+                            rcur[e] = nx;
                         }
                     }
-                } else {  // Ylm of all (l, m)
-                    const float ux = u[0], uy = u[1], t3 = u[2];
-                    float cm[L], sm[L], q1[L], q2[L];
-                    cm[0] = 1.f;
-                    sm[0] = 0.f;
-#pragma unroll
-                    for (int m = 1; m < L; ++m) {
-                        cm[m] = cm[m - 1] * ux - sm[m - 1] * uy;
-                        sm[m] = sm[m - 1] * ux + cm[m - 1] * uy;
+                } else {
+                    const int j = wid - NA4, W2 = 2 * (FWD_THREADS / 32 - NA4);
+                    for (int m = 0; m < L; ++m) {
+                        const int mm = m % W2;
+                        if (mm == j || mm == W2 - 1 - j) ylm_column<float>(m, L, u[0], u[1], u[2], K, tb, Ysm + t * L2);
                     }
-#pragma unroll
-                    for (int m = 0; m < L; ++m) q1[m] = q2[m] = 0.f;
-                    float* Y = Ysm + t * L2;
-#pragma unroll
-                    for (int l = 0; l < L; ++l)
-#pragma unroll
-                        for (int m = 0; m <= l; ++m) {
-                            float q;
-                            if (m == l) {
-                                float qmm = 1.f;
-#pragma unroll
-                                for (int k = 1; k <= 2 * m - 1; k += 2) qmm *= (float)k;
-                                q = qmm;
-                            } else if (m == l - 1) {
-                                q = (float)(2 * m + 1) * t3 * q1[m];
-                            } else {
-                                q = c_lra[l * l + m] * t3 * q1[m] - c_lrbb[l * l + m] * q2[m];
-                            }
-                            q2[m] = q1[m];
-                            q1[m] = q;
-                            const float nq = c_lyn[l * l + m] * q;
-                            if (m == 0) Y[l * l + l] = nq;
-                            else {
-                                Y[l * l + l + m] = nq * cm[m];
-                                Y[l * l + l - m] = nq * sm[m];
-                            }
-                        }
                 }
             }
         }
