@@ -62,6 +62,11 @@ struct Pair2bSet {
 //   displacement (the neighbour build forms d(b->a) = -d(a->b) with sign-symmetric
 //   round-to-nearest steps), so the slots are written in order, without the scattered
 //   read-modify-write of the reverse slot, for twice the (cheap) FP32 exp work.
+// exp of the GP kernel terms: the FP64 path's exp, the fast intrinsic in the FP32 path
+// (relative error ~1e-6 at its arguments, below the FP32 path's other rounding)
+__device__ __forceinline__ double exp_gp(double x) { return exp(x); }
+__device__ __forceinline__ float exp_gp(float x) { return __expf(x); }
+
 template <class R>
 __global__ void k_pair_2b(long long P, const int* __restrict__ Z, const int* __restrict__ mask, const int* __restrict__ ni,
                           const int* __restrict__ nj, const int* __restrict__ ns, const int* __restrict__ rev,
@@ -101,7 +106,7 @@ __global__ void k_pair_2b(long long P, const int* __restrict__ Z, const int* __r
         R e = 0, de = 0;
         for (int s = 0; s < cd.M; ++s) {
             const R t = r - X[s];
-            const R kv = coef[s] * exp(-(R)0.5 * t * t * it2);
+            const R kv = coef[s] * exp_gp(-(R)0.5 * t * t * it2);
             e += kv;
             de -= kv * t * it2;
         }
