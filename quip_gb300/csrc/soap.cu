@@ -25,6 +25,7 @@
 #include <cuda_fp16.h>
 #include <cmath>
 #include <vector>
+#include <climits>
 #include <mutex>
 #include "context.h"
 
@@ -915,6 +916,7 @@ __global__ void __launch_bounds__(BWD_THREADS) k_soap_backward(SoapConst sc, con
 // exp(-alpha r^2) at l = 0 only and is added to the lm = 0 term.
 constexpr int BH_THREADS = 256;
 constexpr int BP_THREADS = 128;
+constexpr int BP_SMEM_BYTES = 32 * 1024;  // h rows a pair-kernel block stages (4 centres at the headline basis)
 constexpr int BH_MAXNN = 24;  // species x n_max of the register-blocked dE/dc rows
 constexpr int MAX_L2 = (MAX_LMAX + 1) * (MAX_LMAX + 1);
 __constant__ float c_lra[MAX_L2], c_lrbb[MAX_L2], c_lyn[MAX_L2];  // by l*l + m, as in the SoapTab
@@ -1163,15 +1165,33 @@ __global__ void __launch_bounds__(BP_THREADS, 3) k_soap_bwd_pairs(SoapConst sc, 
                                                                 const int* __restrict__ a2c, const int* __restrict__ ni,
                                                                 const int* __restrict__ off, const int* __restrict__ Z,
                                                                 const int* __restrict__ nj, const double4* __restrict__ nd,
-                                                                const float* __restrict__ hbuf, double* __restrict__ fpair) {
+                                                                const float* __restrict__ hbuf, double* __restrict__ fpair,
+                                                                int hsm_floats) {
     constexpr int L2 = L * L, NA2 = NMP / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* hsm = reinterpret_cast<float*>(smem_raw);
+    __shared__ int s_cmin, s_cmax;
     const long long p = blockIdx.x * (long long)BP_THREADS + threadIdx.x;
-    if (p >= npair) return;
-    const int ai = ni[p], ci = a2c[ai];
+    const int ai = p < npair ? ni[p] : -1, ci = ai >= 0 ? a2c[ai] : -1;
+    // The block's pairs belong to a few consecutive centres, whose h rows are one contiguous
+    // range of the buffer: copied into shared memory when it fits, else read through L1.
+    const size_t row = (size_t)sc.n_species * L2 * NMP;
+    if (threadIdx.x == 0) { s_cmin = INT_MAX; s_cmax = -1; }
+    __syncthreads();
+    if (ci >= 0) { atomicMin(&s_cmin, ci); atomicMax(&s_cmax, ci); }
+    __syncthreads();
+    const int cmin = s_cmin, nrow = s_cmax - cmin + 1;
+    const bool staged = nrow > 0 && (size_t)nrow * row <= (size_t)hsm_floats;
+    if (staged) {
+        cp_async_floats(hsm, hbuf + (size_t)cmin * row, (int)(nrow * row));
+        cp_async_wait();
+    }
+    __syncthreads();
     if (ci < 0) return;
-    {  // the centre's h block into L1, its 128-byte lines shared out over the centre's pairs
-        const int p0 = off[ai], cnt = off[ai + 1] - p0, lines = (sc.n_species * L2 * NMP * 4 + 127) / 128;
-        const char* hb = reinterpret_cast<const char*>(hbuf + (size_t)ci * sc.n_species * L2 * NMP);
+    const float* hc = staged ? hsm + (size_t)(ci - cmin) * row : hbuf + (size_t)ci * row;
+    if (!staged) {  // the centre's h block into L1, its 128-byte lines shared out over the centre's pairs
+        const int p0 = off[ai], cnt = off[ai + 1] - p0, lines = (int)((row * 4 + 127) / 128);
+        const char* hb = reinterpret_cast<const char*>(hc);
         for (int k = (int)(p - p0); k < lines; k += cnt) asm volatile("prefetch.L1 [%0];" ::"l"(hb + 128 * (size_t)k));
     }
     const double4 d = nd[p];
@@ -1184,7 +1204,7 @@ __global__ void __launch_bounds__(BP_THREADS, 3) k_soap_bwd_pairs(SoapConst sc, 
     const float ux = (float)d.x * ir, uy = (float)d.y * ir, uz = (float)d.z * ir;
     float f, df;
     cutoff_fn<float>(r, (float)sc.rc, (float)sc.w, f, df);
-    const float4* hrow = reinterpret_cast<const float4*>(hbuf + ((size_t)ci * sc.n_species + s) * L2 * NMP);
+    const float4* hrow = reinterpret_cast<const float4*>(hc + (size_t)s * L2 * NMP);
     // radial state: rp = rho_{l-1}, rcur = rho_l (pairs of grid points), ix = 1/x, rbv = rb
     float2 rp[NA2], rcur[NA2];
     float ix[NMP], rbv[NMP];
@@ -1202,7 +1222,7 @@ __global__ void __launch_bounds__(BP_THREADS, 3) k_soap_bwd_pairs(SoapConst sc, 
                 v0 = 0.5f * (em - ep) * xa;
             } else {
                 e0 = em;
-                h0 = __ldg(reinterpret_cast<const float*>(hrow) + a);
+                h0 = reinterpret_cast<const float*>(hrow)[a];
             }
         }
         ix[a] = xa;
@@ -1228,7 +1248,7 @@ __global__ void __launch_bounds__(BP_THREADS, 3) k_soap_bwd_pairs(SoapConst sc, 
         float2 uu = make_float2(0.f, 0.f), vv = make_float2(0.f, 0.f);
 #pragma unroll
         for (int k = 0; k < NMP / 4; ++k) {
-            const float4 h = __ldg(hrow + lm * (NMP / 4) + k);
+            const float4 h = hrow[lm * (NMP / 4) + k];
             const float2 ha = make_float2(h.x, h.y), hb = make_float2(h.z, h.w);
             uu = __ffma2_rn(ha, rcur[2 * k], uu);
             vv = __ffma2_rn(ha, pi[2 * k], vv);
@@ -1674,11 +1694,13 @@ int launch_bwd_pairs(gapgpu_context& c, const Coordinate& co, const SoapConst& s
     const long long P = c.n_pairs;
     if (P == 0) return GAPGPU_OK;
     const unsigned nb = (unsigned)((P + BP_THREADS - 1) / BP_THREADS);
-    k_soap_bwd_pairs<L, NMP><<<nb, BP_THREADS, 0, c.stream>>>(sc, static_cast<const float*>(co.dtab[1]), P, c.a2c.as<int>(),
+    const int hsm_floats = BP_SMEM_BYTES / (int)sizeof(float);
+    GG_CUDA(cudaFuncSetAttribute(k_soap_bwd_pairs<L, NMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, BP_SMEM_BYTES));
+    k_soap_bwd_pairs<L, NMP><<<nb, BP_THREADS, BP_SMEM_BYTES, c.stream>>>(sc, static_cast<const float*>(co.dtab[1]), P, c.a2c.as<int>(),
                                                               c.nbr_i.as<int>(), c.nbr_off.as<int>(), c.Z.as<int>(),
                                                               c.nbr_j.as<int>(),
                                                               c.nbr_d.as<double4>(), c.hbuf.as<float>(),
-                                                              c.fpair.as<double>());
+                                                              c.fpair.as<double>(), hsm_floats);
     c.launches++;
     GG_CUDA(cudaGetLastError());
     return GAPGPU_OK;
