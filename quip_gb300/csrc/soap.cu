@@ -1342,6 +1342,48 @@ __global__ void __launch_bounds__(BP_THREADS, 3) k_soap_bwd_pairs(SoapConst sc, 
 //  * one accumulator item per thread: (species, up to three m of one l, four grid points),
 //    so each staged radial quadruple feeds up to 12 products;
 //  * q, its GEMM-operand copy and c written as vectors.
+// Column m of the real spherical harmonics as ylm_column, with m and L fixed at compile
+// time: the recurrence constants are constant-memory operands and the loop is unrolled.
+__host__ __device__ constexpr float odd_factorial(int m) {
+    float q = 1.f;
+    for (int k = 1; k <= 2 * m - 1; k += 2) q *= (float)k;
+    return q;
+}
+template <int L, int M>
+__device__ __forceinline__ void ylm_col_t(float ux, float uy, float uz, float* Y) {
+    float cm = 1.f, sm = 0.f;
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+        const float c2 = cm * ux - sm * uy;
+        sm = sm * ux + cm * uy;
+        cm = c2;
+    }
+    constexpr float qmm = odd_factorial(M);
+    float q1 = 0.f, q2 = 0.f;
+#pragma unroll
+    for (int l = M; l < L; ++l) {
+        float q;
+        if (l == M) q = qmm;
+        else if (l == M + 1) q = (float)(2 * M + 1) * uz * qmm;
+        else q = c_lra[l * l + M] * uz * q1 - c_lrbb[l * l + M] * q2;
+        q2 = q1;
+        q1 = q;
+        const float nq = c_lyn[l * l + M] * q;
+        if (M == 0) Y[l * l + l] = nq;
+        else {
+            Y[l * l + l + M] = nq * cm;
+            Y[l * l + l - M] = nq * sm;
+        }
+    }
+}
+template <int L, int M = 0>
+__device__ __forceinline__ void ylm_col_dispatch(int m, float ux, float uy, float uz, float* Y) {
+    if constexpr (M < L) {
+        if (m == M) ylm_col_t<L, M>(ux, uy, uz, Y);
+        else ylm_col_dispatch<L, M + 1>(m, ux, uy, uz, Y);
+    }
+}
+
 __host__ __device__ constexpr int fwd_triples(int L) {
     int t = 0;
     for (int l = 0; l < L; ++l) t += (2 * l + 1 + 2) / 3;
@@ -1460,7 +1502,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 4) k_soap_fwd_t(SoapConst sc, con
                     const int j = wid - NA4, W2 = 2 * (FWD_THREADS / 32 - NA4);
                     for (int m = 0; m < L; ++m) {
                         const int mm = m % W2;
-                        if (mm == j || mm == W2 - 1 - j) ylm_column<float>(m, L, u[0], u[1], u[2], K, tb, Ysm + t * L2);
+                        if (mm == j || mm == W2 - 1 - j) ylm_col_dispatch<L>(m, u[0], u[1], u[2], Ysm + t * L2);
                     }
                 }
             }
