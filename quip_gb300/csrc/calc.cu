@@ -174,7 +174,7 @@ void free_model_device(gapgpu_model& m) {
 int prepare_mixed_operands(gapgpu_model& m);  // tcgen05.cu
 
 namespace {
-constexpr int RED_CHUNK = 4096;  // atoms per first-level reduction block (relative to each structure's first atom)
+constexpr int RED_CHUNK = 512;  // atoms per first-level reduction block (relative to each structure's first atom)
 }
 
 // ---------------------------------------------------------------- phase A

@@ -203,7 +203,7 @@ struct EpiParams {
     int izeta;
     void* out_hi;         // W (bf16 hi or tf32 fp32) / G (fp32)
     void* out_lo;         // W lo (bf16x3)
-    double* epart;        // [rows x ntiles]: energies per 64-column block
+    double* epart;        // [ntiles x rows]: energies per 64-column block (rows fastest)
     int ntiles;
     int w_f16;            // EPI_KERNEL, TF32: write W' = wscale K^(zeta-1) as FP16 (for the FP16 second GEMM)
     float wscale;
@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     // energies per 64-column block, whatever the tile width: the sum does not
                     // depend on the autotuner's choice
                     if (cc & 1) {
-                        if (row < ep.rows) ep.epart[(size_t)row * ep.ntiles + (n0 + cc * 32) / 64] = (double)e_acc;
+                        if (row < ep.rows) ep.epart[(size_t)((n0 + cc * 32) / 64) * ep.rows + row] = (double)e_acc;
                         e_acc = 0.f;
                     }
                 }
@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 epilogue_chunk_staged<EPI>(ep, m0 + q * 32, lane, n0 + cc * 32, v, e_acc, epi_stage + q * 1024);
                 if constexpr (EPI == EPI_KERNEL) {
                     if (cc & 1) {
-                        if (row < ep.rows) ep.epart[(size_t)row * ep.ntiles + (n0 + cc * 32) / 64] = (double)e_acc;
+                        if (row < ep.rows) ep.epart[(size_t)((n0 + cc * 32) / 64) * ep.rows + row] = (double)e_acc;
                         e_acc = 0.f;
                     }
                 }
@@ -695,7 +695,7 @@ __global__ void k_rowsum_scatter32(int nc, int ntiles, const double* __restrict_
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
     double s = 0;
-    for (int t = 0; t < ntiles; ++t) s += epart[(size_t)i * ntiles + t];
+    for (int t = 0; t < ntiles; ++t) s += epart[(size_t)t * nc + i];  // [block][row]: rows coalesced
     if (ecent) ecent[i] = s;  // per-centre energies (energy_per_coordinate)
     eatom[centres[i]] += s;
 }
