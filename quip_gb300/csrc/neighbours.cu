@@ -298,12 +298,23 @@ __global__ void k_reverse(long long P, const int* __restrict__ off, const int* _
     if (p >= P) return;
     const int a = ni[p], b = nj[p], s = ns[p];
     const int s0 = (s & 1023) - 512, s1 = ((s >> 10) & 1023) - 512, s2 = ((s >> 20) & 1023) - 512;
+    // one search per unordered pair: the direction with a < b (a == b: the lexicographically
+    // positive image shift) finds its partner and writes both entries
+    if (a > b || (a == b && !(s0 > 0 || (s0 == 0 && (s1 > 0 || (s1 == 0 && s2 > 0)))))) return;
     const int want = pack_shift(-s0, -s1, -s2);
     int found = -1;
     for (int q = off[b]; q < off[b + 1]; ++q)
         if (nj[q] == a && ns[q] == want) { found = q; break; }
     rev[p] = found;
-    if (found < 0) atomicOr(bad, 4);
+    if (found >= 0) rev[found] = (int)p;
+    else atomicOr(bad, 4);
+}
+
+// rev starts at -1 (memset before k_reverse): a pair whose partner direction is missing
+// (an asymmetric list) keeps -1 and sets bit 4 here
+__global__ void k_rev_check(long long P, const int* __restrict__ rev, int* __restrict__ bad) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p < P && rev[p] < 0) atomicOr(bad, 4);
 }
 
 // connection_calc_dists: new displacements for an existing list (same formula as the
@@ -626,11 +637,15 @@ int build_neighbours_batch(gapgpu_context& c, int nstruct, const int* n_atoms, c
                                           c.ms.as<int>(), c.atom_idx2.as<int>(), c.cell_start.as<int>(),
                                           c.cell_end.as<int>(), nullptr, c.nbr_off.as<int>(), c.nbr_j.as<int>(),
                                           c.nbr_d.as<double4>(), c.nbr_s.as<int>(), c.nbr_i.as<int>(), bad);
-    if (tot > 0)
+    if (tot > 0) {
+        GG_CUDA(cudaMemsetAsync(c.nbr_rev.p, 0xff, sizeof(int) * (size_t)tot, st));
         k_reverse<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(tot, c.nbr_off.as<int>(), c.nbr_j.as<int>(),
                                                                   c.nbr_i.as<int>(), c.nbr_s.as<int>(), c.nbr_rev.as<int>(),
                                                                   bad);
-    c.launches += 2;
+        k_rev_check<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(tot, c.nbr_rev.as<int>(), bad);
+        c.launches += 2;
+    }
+    c.launches++;
     int flags = 0;
     GG_CUDA(cudaMemcpyAsync(&flags, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     GG_CUDA(cudaStreamSynchronize(st));
@@ -708,9 +723,11 @@ int load_external_neighbours(gapgpu_context& c, int n, const std::vector<int>& o
         const unsigned nb = (unsigned)((P + 255) / 256);
         k_zero_shift<<<nb, 256, 0, st>>>(P, c.nbr_s.as<int>());
         if ((rc = refresh_distances(c, c.pos.as<double>()))) return rc;
+        GG_CUDA(cudaMemsetAsync(c.nbr_rev.p, 0xff, sizeof(int) * (size_t)P, st));
         k_reverse<<<nb, 256, 0, st>>>(P, c.nbr_off.as<int>(), c.nbr_j.as<int>(), c.nbr_i.as<int>(), c.nbr_s.as<int>(),
                                        c.nbr_rev.as<int>(), bad);
-        c.launches += 2;
+        k_rev_check<<<nb, 256, 0, st>>>(P, c.nbr_rev.as<int>(), bad);
+        c.launches += 3;
     }
     int flags[4] = {0, 0, 0, 0};
     GG_CUDA(cudaMemcpyAsync(flags, c.total.p, sizeof flags, cudaMemcpyDeviceToHost, st));

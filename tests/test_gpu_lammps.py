@@ -85,3 +85,28 @@ def test_lammps_path_empty_region(tmp_path):
     _lib.check(pot._L.gapgpu_calc_lammps(pot._ctx, 0, 3, _lib.ptr(Z), 0, None, None, None, _lib.ptr(lat), _lib.ptr(pos),
                                          _lib.ptr(E), None, None, None, _lib.ptr(F)))
     assert E[0] == 0.0 and np.all(F == 0.0)
+
+
+def test_lammps_path_rejects_an_asymmetric_list(tmp_path):
+    """A local-local pair listed for one atom only: the reverse-pair index finds no partner
+    for the other direction and the call fails with its error, before any force is
+    gathered."""
+    from quip_gb300.potential import Potential
+    path = sic_model(tmp_path)
+    pot = Potential(param_filename=path, precision="fp64")
+    at = models.random_triclinic(60, rng=np.random.default_rng(32))
+    pos, Z, num, neigh, owner = _lammps_view(at, pot.cutoff())
+    n, nloc = len(pos), len(at)
+    first = [k for k in range(num[0]) if neigh[k] - 1 < nloc]   # local neighbours of atom 0
+    assert first
+    neigh = np.delete(neigh, first[-1])
+    num = num.copy()
+    num[0] -= 1
+    ilist = np.arange(nloc, dtype=np.int32)
+    lat = np.asfortranarray(at.lattice).ravel(order="F").copy()
+    E, F, V = np.zeros(1), np.zeros((n, 3)), np.zeros(9)
+    with pytest.raises(_lib.GapGpuError) as e:
+        _lib.check(pot._L.gapgpu_calc_lammps(pot._ctx, nloc, n - nloc, _lib.ptr(Z), nloc, _lib.ptr(ilist), _lib.ptr(num),
+                                             _lib.ptr(neigh), _lib.ptr(lat), _lib.ptr(np.ascontiguousarray(pos)),
+                                             _lib.ptr(E), None, _lib.ptr(V), None, _lib.ptr(F)))
+    assert "symmetric" in str(e.value)
