@@ -738,9 +738,9 @@ def main():
         roofline["kernel"] = ("sparse-GP kernel GEMMs, both launches (tcgen05, tiles chosen by the autotuner): "
                               "K = Q X^T with the fused kernel epilogue, G = W X")
         # DRAM bytes of the two GEMM launches from the ncu capture of the 8192-atom case with
-        # this model (CTA-pair tiles, both GEMMs in FP16: 217+87 MB and 174+32 MB read+written),
+        # this model (CTA-pair tiles, both GEMMs in FP16: 93+93 MB and 176+31 MB read+written),
         # scaled by the row count: the operand re-reads and the W/G traffic grow with the rows
-        roofline["traffic"] = ((217 + 87 + 174 + 32) * 1e6 * n / 8192
+        roofline["traffic"] = ((93 + 93 + 176 + 31) * 1e6 * n / 8192
                                if args.precision == "fp16" and w["kind"] == "sic" and gemm1_f16 and gemm2_f16 else None)
         roofline["traffic_note"] = ("DRAM bytes per step of the two GEMM launches, ncu capture at 8192 atoms scaled by "
                                     "the row count" if roofline["traffic"] else None)
