@@ -131,15 +131,20 @@ __global__ void k_pair_2b(long long P, const int* __restrict__ Z, const int* __r
     }
 }
 
+// GATHER_LANES lanes per atom: lane k takes the atom's pairs k, k + GATHER_LANES, ... in
+// order, and the lanes' sums are combined by an xor butterfly (the same fixed order, and
+// the same bits, in every lane); lane 0 writes.  Deterministic: no atomics.
+constexpr int GATHER_LANES = 4;
 __global__ void k_gather(int n, const int* __restrict__ Z, const int* __restrict__ mask, const int* __restrict__ off,
                          const int* __restrict__ rev, const double4* __restrict__ nd, const double* __restrict__ fpair,
                          const double* __restrict__ epair, const double* __restrict__ eatom, const double* __restrict__ e0,
                          double escale, double* __restrict__ le, double* __restrict__ F, double* __restrict__ LV) {
-    int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
-    double f0 = 0, f1 = 0, f2 = 0, e = eatom[a];
+    const int g = blockIdx.x * blockDim.x + threadIdx.x, a = g / GATHER_LANES, sub = g % GATHER_LANES;
+    const bool ok = a < n;  // lanes past the last atom still take part in the butterfly
+    double f0 = 0, f1 = 0, f2 = 0, e = 0;
     double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int p = off[a]; p < off[a + 1]; ++p) {
+    const int p0 = ok ? off[a] : 0, p1 = ok ? off[a + 1] : 0;
+    for (int p = p0 + sub; p < p1; p += GATHER_LANES) {
         int q = rev[p];
         double4 d = nd[p];
         double g0 = fpair[3 * (size_t)q], g1 = fpair[3 * (size_t)q + 1], g2 = fpair[3 * (size_t)q + 2];
@@ -154,6 +159,17 @@ __global__ void k_gather(int n, const int* __restrict__ Z, const int* __restrict
             for (int r = 0; r < 3; ++r) v[3 * cc + r] += dd[r] * gg[cc];
         e += epair[p] + epair[q];
     }
+#pragma unroll
+    for (int o = 1; o < GATHER_LANES; o <<= 1) {
+        f0 += __shfl_xor_sync(0xffffffffu, f0, o);
+        f1 += __shfl_xor_sync(0xffffffffu, f1, o);
+        f2 += __shfl_xor_sync(0xffffffffu, f2, o);
+        e += __shfl_xor_sync(0xffffffffu, e, o);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    }
+    if (!ok || sub != 0) return;
+    e += eatom[a];
     if (!mask || mask[a]) {
         int z = Z[a];
         e += (z >= 0 && z < 128) ? e0[z] : 0.0;
@@ -355,7 +371,7 @@ int pair_2b(gapgpu_context& c, const std::vector<const Coordinate*>& coords, con
 
 int gather_into(gapgpu_context& c, int n, const double* e0, double escale, double* le, double* F, double* LV) {
     const int TB = 128;
-    k_gather<<<(n + TB - 1) / TB, TB, 0, c.stream>>>(n, c.Z.as<int>(), nullptr, c.nbr_off.as<int>(), c.nbr_rev.as<int>(),
+    k_gather<<<(unsigned)(((size_t)n * GATHER_LANES + TB - 1) / TB), TB, 0, c.stream>>>(n, c.Z.as<int>(), nullptr, c.nbr_off.as<int>(), c.nbr_rev.as<int>(),
                                                     c.nbr_d.as<double4>(), c.fpair.as<double>(), c.epair.as<double>(),
                                                     c.eatom.as<double>(), e0, escale, le, F, LV);
     c.launches++;
@@ -366,7 +382,7 @@ int gather_into(gapgpu_context& c, int n, const double* e0, double escale, doubl
 int gather_outputs(gapgpu_context& c, const gapgpu_model& m, int n, const int* d_mask) {
     const int nchunks = (int)c.h_chunks.size() / 2, ns = c.nstruct;
     const int TB = 128;
-    k_gather<<<(n + TB - 1) / TB, TB, 0, c.stream>>>(n, c.Z.as<int>(), d_mask, c.nbr_off.as<int>(), c.nbr_rev.as<int>(),
+    k_gather<<<(unsigned)(((size_t)n * GATHER_LANES + TB - 1) / TB), TB, 0, c.stream>>>(n, c.Z.as<int>(), d_mask, c.nbr_off.as<int>(), c.nbr_rev.as<int>(),
                                                     c.nbr_d.as<double4>(), c.fpair.as<double>(), c.epair.as<double>(),
                                                     c.eatom.as<double>(), m.de0, m.E_scale, c.out_le.as<double>(),
                                                     c.out_f.as<double>(), c.out_lv.as<double>());

@@ -690,12 +690,17 @@ __global__ void k_to_half(size_t n, const float* __restrict__ in, __half* __rest
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i < n) out[i] = __float2half_rn(in[i]);
 }
+// Energy of each centre from its per-block partials ([block][row]): four lanes per row,
+// lane k summing blocks k, k + 4, ... in order, combined by an xor butterfly (fixed order).
 __global__ void k_rowsum_scatter32(int nc, int ntiles, const double* __restrict__ epart, const int* __restrict__ centres,
                                    double* __restrict__ ecent, double* __restrict__ eatom) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nc) return;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x, i = g >> 2, sub = g & 3;
     double s = 0;
-    for (int t = 0; t < ntiles; ++t) s += epart[(size_t)t * nc + i];  // [block][row]: rows coalesced
+    if (i < nc)
+        for (int t = sub; t < ntiles; t += 4) s += epart[(size_t)t * nc + i];
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (i >= nc || sub != 0) return;
     if (ecent) ecent[i] = s;  // per-centre energies (energy_per_coordinate)
     eatom[centres[i]] += s;
 }
@@ -997,7 +1002,7 @@ int run_mixed(gapgpu_context& c, const Coordinate& co, int nc) {
         rc = gemm<MODE, EPI_KERNEL>(c, c.qlo.p, c.qlo.p, co.dXf32, co.dXf32, nc, Mp, Dp, ep, err, &ntiles);
     if (rc) return rc;
     if (c.want_epc && (rc = c.ecent.ensure(sizeof(double) * (size_t)nc))) return rc;
-    k_rowsum_scatter32<<<(nc + 127) / 128, 128, 0, c.stream>>>(nc, ntiles, c.epart.as<double>(), c.cur_centres,
+    k_rowsum_scatter32<<<(unsigned)((4 * (size_t)nc + 127) / 128), 128, 0, c.stream>>>(nc, ntiles, c.epart.as<double>(), c.cur_centres,
                                                               c.want_epc ? c.ecent.as<double>() : nullptr,
                                                               c.eatom.as<double>());
     c.launches++;
