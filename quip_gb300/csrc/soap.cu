@@ -1161,7 +1161,7 @@ __global__ void k_atom_centre(int nc, const int* __restrict__ centres, int* __re
 }
 
 template <int L, int NMP>
-__global__ void __launch_bounds__(BP_THREADS, 3) k_soap_bwd_pairs(SoapConst sc, const float* __restrict__ tab, long long npair,
+__global__ void __launch_bounds__(BP_THREADS, 4) k_soap_bwd_pairs(SoapConst sc, const float* __restrict__ tab, long long npair,
                                                                 const int* __restrict__ a2c, const int* __restrict__ ni,
                                                                 const int* __restrict__ off, const int* __restrict__ Z,
                                                                 const int* __restrict__ nj, const double4* __restrict__ nd,
@@ -1391,7 +1391,7 @@ __host__ __device__ constexpr int fwd_triples(int L) {
 }
 
 template <int L, int NMP>
-__global__ void __launch_bounds__(FWD_THREADS, 4) k_soap_fwd_t(SoapConst sc, const float* __restrict__ tab, int nc,
+__global__ void __launch_bounds__(FWD_THREADS, 5) k_soap_fwd_t(SoapConst sc, const float* __restrict__ tab, int nc,
                                                              const int* __restrict__ centres, const int* __restrict__ Z,
                                                              const int* __restrict__ off, const int* __restrict__ nj,
                                                              const double4* __restrict__ nd, float* __restrict__ c_out,
