@@ -1,5 +1,6 @@
 """bench.py's host-side arithmetic, without a GPU: the roofline numerator (algorithmic
-FLOPs per atom) and the extrapolation of the sampled CPU baseline to a full structure."""
+FLOPs per atom), the clock summaries of the timed region (nvidia-smi record and NVML
+samples) and the extrapolation of the sampled CPU baseline to a full structure."""
 import time
 
 import numpy as np
@@ -42,6 +43,23 @@ def test_clock_record_summary(tmp_path):
     p.write_text("")
     assert s.keys() >= {"sm_mhz", "sm_max_mhz", "reasons"}
     assert bench.Clocks(str(p)).summary()["sm_mhz"] is None
+
+
+def test_nvml_clock_summary():
+    """The NVML samples (SM MHz, clock-event reason mask) taken during the timed region:
+    median SM clock and every reason bit seen set, by name (0x4 sw_power_cap, 0x8
+    hw_slowdown, 0x20 sw_thermal_slowdown, 0x40 hw_thermal_slowdown); unnamed bits (0x1
+    idle) are left out.  No NVML call is made: the samples are planted."""
+    c = object.__new__(bench.NvmlClocks)
+    c.max_mhz, c.period = 2070.0, 0.01
+    c.samples = []
+    s = c.summary()
+    assert s["sm_mhz"] is None and s["samples"] == 0 and s["sm_max_mhz"] == 2070.0
+    c.samples = [(2070.0, 0x0), (2055.0, 0x4), (2070.0, 0x1), (1980.0, 0x4 | 0x20), (2070.0, 0x0)]
+    s = c.summary()
+    assert s["sm_mhz"] == 2070.0 and s["samples"] == 5
+    assert s["reasons"] == ["sw_power_cap", "sw_thermal_slowdown"]
+    assert "10 ms" in s["source"]
 
 
 class _TimedOracle:
