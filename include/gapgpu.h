@@ -130,13 +130,21 @@ int gapgpu_calc_batch(gapgpu_context* ctx, int nstruct, const int32_t* n_atoms, 
  * GEMM's tile candidates on the first GEMM of each new shape and keep the fastest;
  * "pairs" (0/1/2, default 1, TF32 only): GEMM tiles on CTA pairs (256-row tiles computed
  * by two SMs, tcgen05 cta_group::2) -- 0 never, 1 as autotuner candidates next to the
- * single-CTA tiles (and the choice when no timing is possible), 2 only; "gemm2_f16" (0/1,
+ * single-CTA tiles (and the choice when no timing is possible), 2 only -- contexts whose
+ * calls run at the same time as other contexts' (several streams) should set 0: CTA-pair
+ * GEMMs issued from several streams at once stalled the device under load; "gemm2_f16" (0/1,
  * TF32 and FP16 contexts with pairs; default 1 for GAPGPU_MIXED_F16, 0 for
  * GAPGPU_MIXED_TF32): the second GEMM G = W X in FP16 (W' = S K^(zeta-1) and
  * X' = coef zeta / S x, both 10-bit mantissas in FP16's normal range) where the model
  * allows it (integer zeta, normalised SOAP, bounded S), else in TF32; "gemm1_f16" (0/1,
  * same defaults): the first GEMM K = Q X^T in FP16 as well (FP16 descriptors from the
- * forward kernel and FP16 sparse points, under the same conditions). */
+ * forward kernel and FP16 sparse points, under the same conditions); "soap_fwd" (0/1,
+ * default 1, FP32 SOAP): the forward with the basis size fixed at compile time where the
+ * basis has an instance (l_max + 1 by n_max rounded up to 4: 9x12, 7x8, 5x8, 5x4), else
+ * the generic forward; "soap_bwd" (0/1, default 1, FP32 SOAP): the backward as a
+ * per-centre h kernel followed by one thread per neighbour pair where the basis has an
+ * instance (the same sizes), else one block per centre.  Both choices give the same
+ * results to FP32 rounding. */
 int gapgpu_context_set_option(gapgpu_context* ctx, const char* key, int value);
 
 /* energy_per_coordinate of the last gapgpu_calc / gapgpu_calc_batch whose args requested
